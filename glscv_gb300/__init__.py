@@ -1,0 +1,140 @@
+"""glscv_gb300 -- GB300-native FFT / phaseCorrelate path of glsCV.
+
+The product is the native library ``glscv_gb300/lib/libglscv_gb300.so``
+(hand-written sm_103a CUDA kernels behind the C ABI of ``include/glsfft.h``
+and the C++ ``gls::`` API of ``include/gls/glsCV.h``).  This module is a thin
+ctypes binding used by the tests and the benchmark; it never falls back to
+any other implementation: if the library is missing it raises.
+
+Device buffers are passed as integer addresses (e.g. ``tensor.data_ptr()``);
+streams as integer ``cudaStream_t`` handles (0 = legacy default stream).
+"""
+from __future__ import annotations
+
+import ctypes
+from pathlib import Path
+
+__all__ = [
+    "lib", "GlsError", "Context", "DFT_INVERSE", "DFT_SCALE", "GLS_FFT_SHIFT",
+    "GLS_FFT_INVERSE", "GLS_FFT_SCALE", "LIB_PATH", "HEADER_PATHS",
+]
+
+PKG = Path(__file__).resolve().parent
+LIB_PATH = PKG / "lib" / "libglscv_gb300.so"
+HEADER_PATHS = sorted((PKG.parent / "include").rglob("*.h"))
+
+# flag values of the reference (glsCV/glsFft.h:43-47)
+DFT_INVERSE = GLS_FFT_INVERSE = 1
+DFT_SCALE = GLS_FFT_SCALE = 2
+GLS_FFT_SHIFT = 64
+
+_vp = ctypes.c_void_p
+_ip = ctypes.c_int
+_sz = ctypes.c_size_t
+_dp = ctypes.POINTER(ctypes.c_double)
+
+_SIGNATURES = {
+    "glsfft_status_string": (ctypes.c_char_p, [_ip]),
+    "glsfft_version": (_ip, []),
+    "glsfft_context_create": (_ip, [ctypes.POINTER(_vp), _ip]),
+    "glsfft_context_destroy": (_ip, [_vp]),
+    "glsfft_context_set_budget": (_ip, [_vp, _sz]),
+    "glsfft_context_workspace": (_ip, [_vp, ctypes.POINTER(_sz)]),
+    "glsfft_fft2d_c2c": (_ip, [_vp, _vp, _vp, _ip, _ip, _ip, _vp]),
+    "glsfft_fft2d_r2c_promote": (_ip, [_vp, _vp, _vp, _ip, _ip, _ip, _vp]),
+    "glsfft_phase_correlate": (_ip, [_vp, _vp, _vp, _vp, _ip, _ip, _ip, _dp, _dp, _dp, _vp]),
+    "glsfft_phase_correlate_async": (_ip, [_vp, _vp, _vp, _vp, _ip, _ip, _ip, _vp, _vp]),
+    "glsfft_phase_correlate_surface": (_ip, [_vp, _vp, _sz, _vp]),
+}
+
+_lib = None
+
+
+class GlsError(RuntimeError):
+    """A non-zero status from the C ABI (the reference throws cv::Exception)."""
+
+    def __init__(self, status: int, where: str = ""):
+        self.status = status
+        msg = lib().glsfft_status_string(status).decode()
+        super().__init__(f"{where}: {msg} (status {status})" if where else msg)
+
+
+def lib() -> ctypes.CDLL:
+    """Load the native library (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise RuntimeError(
+                f"{LIB_PATH} is missing: build it with `python -m glscv_gb300.build` "
+                "(there is no fallback implementation)")
+        l = ctypes.CDLL(str(LIB_PATH))
+        for name, (res, args) in _SIGNATURES.items():
+            fn = getattr(l, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = l
+    return _lib
+
+
+def check(status: int, where: str = "") -> None:
+    if status != 0:
+        raise GlsError(status, where)
+
+
+class Context:
+    """Owns a glsfft_context (twiddle tables + workspace) on one device."""
+
+    def __init__(self, device: int = 0):
+        self.handle = _vp()
+        check(lib().glsfft_context_create(ctypes.byref(self.handle), int(device)),
+              "glsfft_context_create")
+        self.device = device
+
+    def close(self) -> None:
+        if self.handle:
+            lib().glsfft_context_destroy(self.handle)
+            self.handle = _vp()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- gls::fft --------------------------------------------------------
+    def fft2d(self, src: int, dst: int, rows: int, cols: int, flags: int = 0,
+              stream: int = 0, real_input: bool = False) -> None:
+        fn = lib().glsfft_fft2d_r2c_promote if real_input else lib().glsfft_fft2d_c2c
+        check(fn(self.handle, src, dst, rows, cols, flags, stream), "fft2d")
+
+    # -- gls::phaseCorrelate -------------------------------------------------
+    def phase_correlate(self, src1: int, src2: int, window: int | None, rows: int, cols: int,
+                        box: int = 5, stream: int = 0):
+        dx, dy, resp = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        check(lib().glsfft_phase_correlate(self.handle, src1, src2, window or None, rows, cols,
+                                           box, ctypes.byref(dx), ctypes.byref(dy),
+                                           ctypes.byref(resp), stream), "phase_correlate")
+        return (dx.value, dy.value), resp.value
+
+    def phase_correlate_async(self, src1: int, src2: int, window: int | None, rows: int,
+                              cols: int, box: int, d_result: int, stream: int = 0) -> None:
+        check(lib().glsfft_phase_correlate_async(self.handle, src1, src2, window or None, rows,
+                                                 cols, box, d_result, stream),
+              "phase_correlate_async")
+
+    def copy_surface(self, dst: int, count: int, stream: int = 0) -> None:
+        check(lib().glsfft_phase_correlate_surface(self.handle, dst, count, stream), "surface")
+
+    def workspace_bytes(self) -> int:
+        b = _sz()
+        check(lib().glsfft_context_workspace(self.handle, ctypes.byref(b)), "workspace")
+        return b.value
+
+    def set_budget(self, nbytes: int) -> None:
+        check(lib().glsfft_context_set_budget(self.handle, nbytes), "set_budget")

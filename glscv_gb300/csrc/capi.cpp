@@ -1,0 +1,362 @@
+// capi.cpp -- the C ABI of include/glsfft.h: argument checks, the context
+// (twiddle tables + workspace) and the launch sequences of gls::fft and
+// gls::phaseCorrelate.
+#include "glsfft.h"
+
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <vector>
+
+#include "capi_internal.h"
+#include "glsfft_internal.h"
+
+using namespace glsfft;
+
+// --------------------------------------------------------------- twiddles
+// e^{-2 pi i k/n}, k < n, from an exact quadrant / octant reduction so that
+// +-1, 0 and the pi/4 values come out exact and symmetric; FP64, then one
+// rounding to FP32.
+void glsfft::make_twiddle_host(float2 *dst) {
+    const double two_pi = 6.283185307179586476925286766559;
+    for (int n = 2; n <= kMaxLen; n <<= 1) {
+        for (int k = 0; k < n; k++) {
+            const int q = (4 * k) / n;        // quadrant
+            const int r = k - q * (n / 4);    // position inside the quadrant
+            double c, s;                      // cos, sin of 2 pi r / n
+            if (n < 4) {
+                c = (k == 0) ? 1.0 : -1.0;
+                s = 0.0;
+            } else if (8 * r <= n) {
+                c = std::cos(two_pi * r / n);
+                s = std::sin(two_pi * r / n);
+            } else {
+                const double a = two_pi * (n / 4 - r) / n;
+                c = std::sin(a);
+                s = std::cos(a);
+            }
+            double cr = c, sr = s;  // rotate by i^q
+            if (n >= 4) {
+                for (int i = 0; i < q; i++) {
+                    const double t = cr;
+                    cr = -sr;
+                    sr = t;
+                }
+            }
+            // forward sign: e^{-i theta} = cos - i sin
+            dst[n + k] = make_float2((float)cr, (float)(-sr));
+        }
+    }
+}
+
+// ---------------------------------------------------------------- helpers
+namespace {
+
+inline bool is_pow2(int x) { return x > 0 && (x & (x - 1)) == 0; }
+
+int check_dims(int rows, int cols) {
+    if (rows < 1 || cols < 1 || rows > kMaxLen || cols > kMaxLen) return GLSFFT_ERROR_SIZE;
+    if (!is_pow2(rows) || !is_pow2(cols)) return GLSFFT_ERROR_NOT_POW2;
+    return GLSFFT_SUCCESS;
+}
+
+inline bool aligned(const void *p, size_t a) { return (reinterpret_cast<uintptr_t>(p) % a) == 0; }
+
+}  // namespace
+
+int glsfft::cuda_status(cudaError_t e) {
+    if (e == cudaSuccess) return GLSFFT_SUCCESS;
+    if (e == cudaErrorMemoryAllocation) return GLSFFT_ERROR_OUT_OF_MEMORY;
+    return GLSFFT_ERROR_CUDA;
+}
+
+DeviceGuard::DeviceGuard(int dev) {
+    if (cudaGetDevice(&prev_) != cudaSuccess) prev_ = -1;
+    if (prev_ != dev) ok_ = cudaSetDevice(dev) == cudaSuccess;
+}
+DeviceGuard::~DeviceGuard() {
+    int cur = -1;
+    if (prev_ >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev_) cudaSetDevice(prev_);
+}
+
+int glsfft::ensure_workspace(glsfft_context ctx, size_t bytes) {
+    if (bytes <= ctx->ws_bytes) return GLSFFT_SUCCESS;
+    if (ctx->budget && bytes > ctx->budget) return GLSFFT_ERROR_BUDGET;
+    if (ctx->ws) {
+        cudaError_t e = cudaFree(ctx->ws);
+        ctx->ws = nullptr;
+        ctx->ws_bytes = 0;
+        if (e != cudaSuccess) return cuda_status(e);
+    }
+    void *p = nullptr;
+    cudaError_t e = cudaMalloc(&p, bytes);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return GLSFFT_ERROR_OUT_OF_MEMORY;
+    }
+    ctx->ws = p;
+    ctx->ws_bytes = bytes;
+    return GLSFFT_SUCCESS;
+}
+
+// The two passes of gls::fft.  `real_in`: src is CV_32FC1 (promote).
+int glsfft::fft2d_launch(glsfft_context ctx, const void *src, void *dst, int rows, int cols,
+                         int flags, bool real_in, cudaStream_t s) {
+    const bool inv = flags & GLSFFT_INVERSE, scale = flags & GLSFFT_SCALE,
+               shift = flags & GLSFFT_SHIFT;
+    const bool do_rows = cols > 1 || rows == 1 || real_in;
+    const bool do_cols = rows > 1;
+    if (do_rows) {
+        PassArgs a{};
+        a.in0 = src;
+        a.out0 = dst;
+        a.rows = rows;
+        a.cols = cols;
+        a.scale = scale ? 1.0f / (float)cols : 1.0f;
+        a.flags = (inv ? PF_CONJ_IN : 0u) | (inv && !do_cols ? PF_CONJ_OUT : 0u) |
+                  (shift ? PF_SHIFT_COLS : 0u);
+        a.tw = ctx->d_tw + cols;
+        cudaError_t e = launch_rows(cols, real_in ? LD_R1 : LD_C2, ST_C2, a, 1, s);
+        if (e != cudaSuccess) return cuda_status(e);
+    }
+    if (do_cols) {
+        PassArgs a{};
+        a.in0 = do_rows ? dst : src;
+        a.out0 = dst;
+        a.rows = rows;
+        a.cols = cols;
+        a.scale = scale ? 1.0f / (float)rows : 1.0f;
+        a.flags = (inv && !do_rows ? PF_CONJ_IN : 0u) | (inv ? PF_CONJ_OUT : 0u) |
+                  (shift ? PF_SHIFT_ROWS : 0u);
+        a.tw = ctx->d_tw + rows;
+        cudaError_t e = launch_cols(rows, LD_C2, ST_C2, a, 1, s);
+        if (e != cudaSuccess) return cuda_status(e);
+    }
+    return GLSFFT_SUCCESS;
+}
+
+// phaseCorrelate launch sequence on caller-provided scratch:
+// f1, f2: rows*cols complex each; surface: rows*cols floats; key: 8 bytes.
+int glsfft::poc_launch(const float2 *tw, const float *src1, const float *src2,
+                       const float *window, int rows, int cols, int box, float2 *f1, float2 *f2,
+                       float *surface, unsigned long long *key, double *d_result,
+                       cudaStream_t s) {
+    cudaError_t e = cudaMemsetAsync(key, 0, sizeof(unsigned long long), s);
+    if (e != cudaSuccess) return cuda_status(e);
+    PassArgs a{};
+    a.in0 = src1;
+    a.in1 = src2;
+    a.out0 = f1;
+    a.out1 = f2;
+    a.window = window;
+    a.rows = rows;
+    a.cols = cols;
+    a.scale = 1.0f;
+    a.tw = tw + cols;
+    e = launch_rows(cols, window ? LD_R1W : LD_R1, ST_C2, a, 2, s);
+    if (e != cudaSuccess) return cuda_status(e);
+
+    PassArgs b{};
+    b.in0 = f1;
+    b.in1 = f2;
+    b.out0 = f1;
+    b.rows = rows;
+    b.cols = cols;
+    b.scale = 1.0f;
+    b.tw = tw + rows;
+    e = launch_poc_cols(rows, b, s);
+    if (e != cudaSuccess) return cuda_status(e);
+
+    PassArgs c{};
+    c.in0 = f1;
+    c.out0 = surface;
+    c.rows = rows;
+    c.cols = cols;
+    c.scale = 1.0f;
+    c.flags = PF_SHIFT_ROWS | PF_SHIFT_COLS;
+    c.key = key;
+    c.tw = tw + cols;
+    e = launch_rows(cols, LD_C2, ST_RE_ARGMAX, c, 1, s);
+    if (e != cudaSuccess) return cuda_status(e);
+
+    e = launch_poc_finish(surface, rows, cols, box, key, d_result, s);
+    return cuda_status(e);
+}
+
+int glsfft::check_poc_args(glsfft_context ctx, const float *src1, const float *src2,
+                           const float *window, int rows, int cols, int box) {
+    if (!src1 || !src2) return GLSFFT_ERROR_INVALID_VALUE;
+    int st = check_dims(rows, cols);
+    if (st) return st;
+    if (box < 1) return GLSFFT_ERROR_INVALID_VALUE;
+    if (!aligned(src1, 4) || !aligned(src2, 4) || (window && !aligned(window, 4)))
+        return GLSFFT_ERROR_MISALIGNED;
+    if (!ctx) return GLSFFT_ERROR_INVALID_VALUE;
+    return GLSFFT_SUCCESS;
+}
+
+int glsfft::check_fft_args(const void *src, const void *dst, int rows, int cols, int flags,
+                           bool real_in) {
+    if (!src || !dst) return GLSFFT_ERROR_INVALID_VALUE;
+    if (flags & ~(GLSFFT_INVERSE | GLSFFT_SCALE | GLSFFT_SHIFT)) return GLSFFT_ERROR_INVALID_VALUE;
+    int st = check_dims(rows, cols);
+    if (st) return st;
+    if (!aligned(src, real_in ? 4 : 8) || !aligned(dst, 8)) return GLSFFT_ERROR_MISALIGNED;
+    return GLSFFT_SUCCESS;
+}
+
+// ------------------------------------------------------------------ C ABI
+extern "C" {
+
+const char *glsfft_status_string(int status) {
+    switch (status) {
+    case GLSFFT_SUCCESS: return "success";
+    case GLSFFT_ERROR_INVALID_VALUE: return "invalid value (NULL pointer or handle, unknown flag, bad box)";
+    case GLSFFT_ERROR_NOT_POW2: return "size is not a power of two";
+    case GLSFFT_ERROR_SIZE: return "size outside [1, GLSFFT_MAX_LEN]";
+    case GLSFFT_ERROR_MISALIGNED: return "pointer not aligned to its element size";
+    case GLSFFT_ERROR_CUDA: return "CUDA runtime error";
+    case GLSFFT_ERROR_OUT_OF_MEMORY: return "device memory allocation failed";
+    case GLSFFT_ERROR_BUDGET: return "workspace would exceed the context's HBM budget";
+    case GLSFFT_ERROR_TIMEOUT: return "bounded device-side wait expired";
+    case GLSFFT_ERROR_SHAPE: return "inputs have different shapes";
+    default: return "unknown status";
+    }
+}
+
+int glsfft_version(void) { return 100; }
+
+int glsfft_context_create(glsfft_context *out, int device) {
+    if (!out) return GLSFFT_ERROR_INVALID_VALUE;
+    *out = nullptr;
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return GLSFFT_ERROR_CUDA;
+    }
+    if (device < 0 || device >= ndev) return GLSFFT_ERROR_INVALID_VALUE;
+    DeviceGuard g(device);
+    if (!g.ok()) return GLSFFT_ERROR_CUDA;
+    auto *ctx = new (std::nothrow) glsfft_context_s();
+    if (!ctx) return GLSFFT_ERROR_OUT_OF_MEMORY;
+    ctx->device = device;
+    std::vector<float2> tw(2 * (size_t)kMaxLen);
+    make_twiddle_host(tw.data());
+    e = cudaMalloc(&ctx->d_tw, sizeof(float2) * tw.size());
+    if (e == cudaSuccess)
+        e = cudaMemcpy(ctx->d_tw, tw.data(), sizeof(float2) * tw.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMallocHost(&ctx->h_result, 8 * sizeof(double));
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        if (ctx->d_tw) cudaFree(ctx->d_tw);
+        delete ctx;
+        return cuda_status(e);
+    }
+    *out = ctx;
+    return GLSFFT_SUCCESS;
+}
+
+int glsfft_context_destroy(glsfft_context ctx) {
+    if (!ctx) return GLSFFT_ERROR_INVALID_VALUE;
+    DeviceGuard g(ctx->device);
+    if (ctx->ws) cudaFree(ctx->ws);
+    if (ctx->d_tw) cudaFree(ctx->d_tw);
+    if (ctx->h_result) cudaFreeHost(ctx->h_result);
+    delete ctx;
+    return GLSFFT_SUCCESS;
+}
+
+int glsfft_context_set_budget(glsfft_context ctx, size_t bytes) {
+    if (!ctx) return GLSFFT_ERROR_INVALID_VALUE;
+    ctx->budget = bytes;
+    return GLSFFT_SUCCESS;
+}
+
+int glsfft_context_workspace(glsfft_context ctx, size_t *bytes) {
+    if (!ctx || !bytes) return GLSFFT_ERROR_INVALID_VALUE;
+    *bytes = ctx->ws_bytes;
+    return GLSFFT_SUCCESS;
+}
+
+int glsfft_fft2d_c2c(glsfft_context ctx, const void *src, void *dst, int rows, int cols,
+                     int flags, void *stream) {
+    int st = check_fft_args(src, dst, rows, cols, flags, false);
+    if (st) return st;
+    if (!ctx) return GLSFFT_ERROR_INVALID_VALUE;
+    DeviceGuard g(ctx->device);
+    if (!g.ok()) return GLSFFT_ERROR_CUDA;
+    return fft2d_launch(ctx, src, dst, rows, cols, flags, false, (cudaStream_t)stream);
+}
+
+int glsfft_fft2d_r2c_promote(glsfft_context ctx, const float *src, void *dst, int rows,
+                             int cols, int flags, void *stream) {
+    int st = check_fft_args(src, dst, rows, cols, flags, true);
+    if (st) return st;
+    if (!ctx) return GLSFFT_ERROR_INVALID_VALUE;
+    DeviceGuard g(ctx->device);
+    if (!g.ok()) return GLSFFT_ERROR_CUDA;
+    return fft2d_launch(ctx, src, dst, rows, cols, flags, true, (cudaStream_t)stream);
+}
+
+int glsfft_phase_correlate_async(glsfft_context ctx, const float *src1, const float *src2,
+                                 const float *window, int rows, int cols, int box,
+                                 double *d_result, void *stream) {
+    int st = check_poc_args(ctx, src1, src2, window, rows, cols, box);
+    if (st) return st;
+    if (!d_result) return GLSFFT_ERROR_INVALID_VALUE;
+    if (!aligned(d_result, 8)) return GLSFFT_ERROR_MISALIGNED;
+    DeviceGuard g(ctx->device);
+    if (!g.ok()) return GLSFFT_ERROR_CUDA;
+    const size_t n = (size_t)rows * cols;
+    const size_t bytes = poc_workspace_bytes(rows, cols);
+    st = ensure_workspace(ctx, bytes);
+    if (st) return st;
+    char *ws = static_cast<char *>(ctx->ws);
+    float2 *f1 = reinterpret_cast<float2 *>(ws);
+    float2 *f2 = f1 + n;
+    float *surface = reinterpret_cast<float *>(f2 + n);
+    auto *key = reinterpret_cast<unsigned long long *>(ws + poc_key_offset(rows, cols));
+    ctx->surface = surface;
+    ctx->surface_count = n;
+    return poc_launch(ctx->d_tw, src1, src2, window, rows, cols, box, f1, f2, surface, key,
+                      d_result, (cudaStream_t)stream);
+}
+
+int glsfft_phase_correlate(glsfft_context ctx, const float *src1, const float *src2,
+                           const float *window, int rows, int cols, int box, double *dx,
+                           double *dy, double *response, void *stream) {
+    if (!dx || !dy) return GLSFFT_ERROR_INVALID_VALUE;
+    int st = check_poc_args(ctx, src1, src2, window, rows, cols, box);
+    if (st) return st;
+    DeviceGuard g(ctx->device);
+    if (!g.ok()) return GLSFFT_ERROR_CUDA;
+    st = ensure_workspace(ctx, poc_workspace_bytes(rows, cols));
+    if (st) return st;
+    double *d_res = reinterpret_cast<double *>(static_cast<char *>(ctx->ws) +
+                                               poc_result_offset(rows, cols));
+    st = glsfft_phase_correlate_async(ctx, src1, src2, window, rows, cols, box, d_res, stream);
+    if (st) return st;
+    cudaStream_t s = (cudaStream_t)stream;
+    cudaError_t e = cudaMemcpyAsync(ctx->h_result, d_res, 5 * sizeof(double),
+                                    cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cuda_status(e);
+    *dx = ctx->h_result[0];
+    *dy = ctx->h_result[1];
+    if (response) *response = ctx->h_result[2];
+    return GLSFFT_SUCCESS;
+}
+
+int glsfft_phase_correlate_surface(glsfft_context ctx, float *dst, size_t count, void *stream) {
+    if (!ctx || !dst) return GLSFFT_ERROR_INVALID_VALUE;
+    if (!ctx->surface || count != ctx->surface_count) return GLSFFT_ERROR_SHAPE;
+    DeviceGuard g(ctx->device);
+    if (!g.ok()) return GLSFFT_ERROR_CUDA;
+    return cuda_status(cudaMemcpyAsync(dst, ctx->surface, count * sizeof(float),
+                                       cudaMemcpyDeviceToDevice, (cudaStream_t)stream));
+}
+
+}  // extern "C"

@@ -1,0 +1,53 @@
+// capi_internal.h -- the context object and host helpers shared by the C ABI
+// translation units.  Not a public header.
+#pragma once
+#include <cuda_runtime.h>
+#include <stddef.h>
+
+#include "glsfft.h"
+
+struct glsfft_context_s {
+    int device = 0;
+    float2 *d_tw = nullptr;     // twiddle tables, see make_twiddle_host
+    void *ws = nullptr;         // workspace (phaseCorrelate scratch)
+    size_t ws_bytes = 0;
+    size_t budget = 0;          // 0 = unlimited
+    double *h_result = nullptr; // pinned, 8 doubles
+    const float *surface = nullptr;  // last phaseCorrelate surface
+    size_t surface_count = 0;
+};
+
+namespace glsfft {
+
+// Sets the device for the scope of a call and restores the caller's.
+class DeviceGuard {
+  public:
+    explicit DeviceGuard(int dev);
+    ~DeviceGuard();
+    bool ok() const { return ok_; }
+
+  private:
+    int prev_ = -1;
+    bool ok_ = true;
+};
+
+int cuda_status(cudaError_t e);
+int ensure_workspace(glsfft_context ctx, size_t bytes);
+int check_fft_args(const void *src, const void *dst, int rows, int cols, int flags, bool real_in);
+int check_poc_args(glsfft_context ctx, const float *src1, const float *src2,
+                   const float *window, int rows, int cols, int box);
+int fft2d_launch(glsfft_context ctx, const void *src, void *dst, int rows, int cols, int flags,
+                 bool real_in, cudaStream_t s);
+int poc_launch(const float2 *tw, const float *src1, const float *src2, const float *window,
+               int rows, int cols, int box, float2 *f1, float2 *f2, float *surface,
+               unsigned long long *key, double *d_result, cudaStream_t s);
+
+// phaseCorrelate workspace: f1 | f2 (complex) | surface (float) | key | result
+inline size_t poc_key_offset(int rows, int cols) {
+    const size_t n = (size_t)rows * cols;
+    return (20 * n + 255) / 256 * 256;
+}
+inline size_t poc_result_offset(int rows, int cols) { return poc_key_offset(rows, cols) + 64; }
+inline size_t poc_workspace_bytes(int rows, int cols) { return poc_result_offset(rows, cols) + 64; }
+
+}  // namespace glsfft

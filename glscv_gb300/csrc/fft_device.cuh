@@ -1,0 +1,233 @@
+// fft_device.cuh -- device building blocks of the GB300 FFT path.
+//
+// One power-of-two FFT "line" (a row or a column of a CV_32FC2 image) is
+// computed by T = N/E threads, each holding E complex values in registers.
+// Passes are Stockham autosort radix-R steps (R in {2,4,8,16}, balanced so
+// that ceil(log2 N / 4) passes suffice).  The first pass takes its operands
+// straight from the global load, the last pass leaves results in the same
+// registers in natural order for the global store, and the passes in between
+// exchange through shared memory, so a line costs one global read and one
+// global write.  This replaces the reference's one-draw-per-radix-4-pass
+// fragment shader (glsCV/glsFft.cpp:203-343) and its ping-pong textures
+// (glsFft.cpp:528-532).
+//
+// Register slot m of thread t always holds line position t + m*T on entry to
+// a pass; in a pass with radix R and span Ns, butterfly j = t + s*T
+// (s < E/R) reads slots s + r*E/R (positions j + r*N/R), twiddles by
+// w_N^{(j mod Ns) * r * N/(Ns*R)}, runs an R-point DFT and writes positions
+// (j/Ns)*Ns*R + (j mod Ns) + r*Ns.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace glsfft {
+
+// ------------------------------------------------------------ complex helpers
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+    return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ float2 cconj(float2 a) { return make_float2(a.x, -a.y); }
+__device__ __forceinline__ float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
+
+// --------------------------------------------------------- radix schedule
+__host__ __device__ constexpr int ilog2c(int n) { return n <= 1 ? 0 : 1 + ilog2c(n >> 1); }
+__host__ __device__ constexpr int num_passes(int n) {
+    return ilog2c(n) == 0 ? 0 : (ilog2c(n) <= 4 ? 1 : (ilog2c(n) + 3) / 4);
+}
+__host__ __device__ constexpr int pass_bits(int n, int p) {
+    return ilog2c(n) / num_passes(n) + (p < ilog2c(n) % num_passes(n) ? 1 : 0);
+}
+__host__ __device__ constexpr int pass_radix(int n, int p) { return 1 << pass_bits(n, p); }
+__host__ __device__ constexpr int pass_span(int n, int p) {
+    return p == 0 ? 1 : pass_span(n, p - 1) * pass_radix(n, p - 1);
+}
+__host__ __device__ constexpr int max_radix(int n) { return num_passes(n) == 0 ? 1 : pass_radix(n, 0); }
+
+// ------------------------------------------- multiply by w_R^K = e^{-2 pi i K/R}
+// Exact special cases for multiples of pi/4; cos/sin(pi/8) constants otherwise.
+template <int K, int R>
+__device__ __forceinline__ float2 wmul(float2 v) {
+    constexpr int k16 = ((K % R) + R) % R * (16 / R);
+    constexpr float S = 0.70710678118654752440f;  // sqrt(1/2)
+    constexpr float C1 = 0.92387953251128675613f; // cos(pi/8)
+    constexpr float S1 = 0.38268343236508977173f; // sin(pi/8)
+    if constexpr (k16 == 0) return v;
+    else if constexpr (k16 == 4) return make_float2(v.y, -v.x);
+    else if constexpr (k16 == 8) return make_float2(-v.x, -v.y);
+    else if constexpr (k16 == 12) return make_float2(-v.y, v.x);
+    else if constexpr (k16 == 2) return make_float2((v.x + v.y) * S, (v.y - v.x) * S);
+    else if constexpr (k16 == 6) return make_float2((v.y - v.x) * S, -(v.x + v.y) * S);
+    else if constexpr (k16 == 10) return make_float2(-(v.x + v.y) * S, (v.x - v.y) * S);
+    else if constexpr (k16 == 14) return make_float2((v.x - v.y) * S, (v.x + v.y) * S);
+    else {
+        // odd multiples of pi/8: e^{-i k pi/8}
+        constexpr float c = (k16 == 1 || k16 == 15) ? C1 : (k16 == 3 || k16 == 13) ? S1
+                          : (k16 == 5 || k16 == 11) ? -S1 : -C1;
+        constexpr float s = (k16 == 1 || k16 == 7) ? -S1 : (k16 == 3 || k16 == 5) ? -C1
+                          : (k16 == 9 || k16 == 15) ? S1 : C1;
+        return make_float2(v.x * c - v.y * s, v.x * s + v.y * c);
+    }
+}
+
+// ------------------------------------------------ R-point DFTs in registers
+// In place, natural-order output, forward sign.
+template <int R> struct Dft;
+template <> struct Dft<1> { __device__ __forceinline__ static void run(float2 *) {} };
+template <> struct Dft<2> {
+    __device__ __forceinline__ static void run(float2 *v) {
+        float2 a = v[0], b = v[1];
+        v[0] = cadd(a, b);
+        v[1] = csub(a, b);
+    }
+};
+template <> struct Dft<4> {
+    __device__ __forceinline__ static void run(float2 *v) {
+        float2 apc = cadd(v[0], v[2]), amc = csub(v[0], v[2]);
+        float2 bpd = cadd(v[1], v[3]), bmd = csub(v[1], v[3]);
+        v[0] = cadd(apc, bpd);
+        v[2] = csub(apc, bpd);
+        v[1] = make_float2(amc.x + bmd.y, amc.y - bmd.x);  // amc - i*bmd
+        v[3] = make_float2(amc.x - bmd.y, amc.y + bmd.x);  // amc + i*bmd
+    }
+};
+template <> struct Dft<8> {
+    __device__ __forceinline__ static void run(float2 *v) {
+        float2 e[4] = {v[0], v[2], v[4], v[6]};
+        float2 o[4] = {v[1], v[3], v[5], v[7]};
+        Dft<4>::run(e);
+        Dft<4>::run(o);
+        o[1] = wmul<1, 8>(o[1]);
+        o[2] = wmul<2, 8>(o[2]);
+        o[3] = wmul<3, 8>(o[3]);
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            v[k] = cadd(e[k], o[k]);
+            v[k + 4] = csub(e[k], o[k]);
+        }
+    }
+};
+template <> struct Dft<16> {
+    __device__ __forceinline__ static void run(float2 *v) {
+        float2 a0[4] = {v[0], v[4], v[8], v[12]};
+        float2 a1[4] = {v[1], v[5], v[9], v[13]};
+        float2 a2[4] = {v[2], v[6], v[10], v[14]};
+        float2 a3[4] = {v[3], v[7], v[11], v[15]};
+        Dft<4>::run(a0);
+        Dft<4>::run(a1);
+        Dft<4>::run(a2);
+        Dft<4>::run(a3);
+        a1[1] = wmul<1, 16>(a1[1]); a1[2] = wmul<2, 16>(a1[2]); a1[3] = wmul<3, 16>(a1[3]);
+        a2[1] = wmul<2, 16>(a2[1]); a2[2] = wmul<4, 16>(a2[2]); a2[3] = wmul<6, 16>(a2[3]);
+        a3[1] = wmul<3, 16>(a3[1]); a3[2] = wmul<6, 16>(a3[2]); a3[3] = wmul<9, 16>(a3[3]);
+#pragma unroll
+        for (int k1 = 0; k1 < 4; k1++) {
+            float2 b[4] = {a0[k1], a1[k1], a2[k1], a3[k1]};
+            Dft<4>::run(b);
+            v[k1] = b[0];
+            v[k1 + 4] = b[1];
+            v[k1 + 8] = b[2];
+            v[k1 + 12] = b[3];
+        }
+    }
+};
+
+// ------------------------------------------------------- the line engine
+// Sm: shared-memory accessor, sm(pos) -> float2& for this thread's line.
+// tw: twiddle table for length N, tw[k] = e^{-2 pi i k/N}, k < N.
+template <int N, int E>
+struct LineFft {
+    static_assert((N & (N - 1)) == 0 && N >= 1 && N <= 8192, "N must be a power of two");
+    static_assert(N == 1 || (N % E) == 0, "E must divide N");
+    static constexpr int T = (N >= E) ? N / E : 1;
+    static constexpr int P = num_passes(N);
+
+    template <class Sm>
+    __device__ __forceinline__ static void run(float2 (&x)[E], int t, Sm sm,
+                                               const float2 *__restrict__ tw) {
+        pass<0>(x, t, sm, tw);
+    }
+
+    template <int p, class Sm>
+    __device__ __forceinline__ static void pass(float2 (&x)[E], int t, Sm sm,
+                                                const float2 *__restrict__ tw) {
+        if constexpr (p < P) {
+            constexpr int R = pass_radix(N, p);
+            constexpr int Ns = pass_span(N, p);
+            constexpr int S = E / R;
+            constexpr bool last = (Ns * R == N);
+            static_assert(E % R == 0, "E must be a multiple of every radix");
+#pragma unroll
+            for (int s = 0; s < S; s++) {
+                const int j = t + s * T;
+                float2 v[R];
+#pragma unroll
+                for (int r = 0; r < R; r++) v[r] = x[s + r * S];
+                if constexpr (Ns > 1) {
+                    const int k = j & (Ns - 1);
+                    constexpr int step = N / (Ns * R);
+#pragma unroll
+                    for (int r = 1; r < R; r++) v[r] = cmul(v[r], __ldg(tw + k * r * step));
+                }
+                Dft<R>::run(v);
+                if constexpr (last) {
+#pragma unroll
+                    for (int r = 0; r < R; r++) x[s + r * S] = v[r];
+                } else {
+                    const int d = (j / Ns) * Ns * R + (j & (Ns - 1));
+#pragma unroll
+                    for (int r = 0; r < R; r++) sm(d + r * Ns) = v[r];
+                }
+            }
+            if constexpr (!last) {
+                __syncthreads();
+#pragma unroll
+                for (int m = 0; m < E; m++) x[m] = sm(t + m * T);
+                __syncthreads();
+                pass<p + 1>(x, t, sm, tw);
+            }
+        }
+    }
+};
+
+// --------------------------------------------------- argmax key (first max)
+// Max value wins; equal values resolve to the smaller row-major index, which
+// is the first occurrence the reference's strict '>' scans keep
+// (glsCV/glsMinMaxLoc.cpp:91, :109).  NaN and values <= -FLT_MAX never win.
+__device__ __forceinline__ unsigned long long argmax_key(float v, unsigned idx) {
+    if (!(v > -3.402823466e+38f)) return 0ull;
+    unsigned b = __float_as_uint(v);
+    unsigned o = (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+    return ((unsigned long long)o << 32) | (unsigned long long)(0xFFFFFFFFu - idx);
+}
+__device__ __forceinline__ float key_value(unsigned long long key) {
+    unsigned o = (unsigned)(key >> 32);
+    unsigned b = (o & 0x80000000u) ? (o & 0x7FFFFFFFu) : ~o;
+    return __uint_as_float(b);
+}
+__device__ __forceinline__ unsigned key_index(unsigned long long key) {
+    return 0xFFFFFFFFu - (unsigned)(key & 0xFFFFFFFFull);
+}
+
+// Block-wide max of keys; thread 0 issues one atomicMax.  `red` needs
+// blockDim.x/32 entries of shared memory.
+__device__ __forceinline__ void block_argmax_commit(unsigned long long key,
+                                                    unsigned long long *red,
+                                                    unsigned long long *dst) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        unsigned long long o = __shfl_xor_sync(0xffffffffu, key, off);
+        key = o > key ? o : key;
+    }
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) red[warp] = key;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long best = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) best = red[w] > best ? red[w] : best;
+        if (best) atomicMax(dst, best);
+    }
+}
+
+}  // namespace glsfft

@@ -1,0 +1,212 @@
+// fft_kernels.cuh -- row-pass and column-pass kernels of the 2-D FFT and the
+// fused phaseCorrelate kernels, as templates over the line length N.
+//
+// Reference semantics (glsCV, paths inside that project):
+//   gls::fft rows-then-columns Stockham       glsCV/glsFft.cpp:494-671
+//   INVERSE = conj in (first pass) / conj out (last pass)   :600, :646
+//   SCALE = x 1/N of that dimension at its last stage        :601, :647
+//   SHIFT = quadrant swap of the output                      :656-664
+//   1-channel input promoted to complex, imag = 0            :684-689
+//   window multiply before the FFT       glsCV/glsPhaseCorrelate.cpp:178-184
+//   phase-only spectrum, no epsilon      glsCV/glsBasicOperation.cpp:195-206
+//   real part of the inverse             glsCV/glsPhaseCorrelate.cpp:202-204
+//   first-occurrence argmax              glsCV/glsMinMaxLoc.cpp:65-119
+//   FP64 weighted centroid, clamped box  glsCV/glsPhaseCorrelate.cpp:60-137
+#pragma once
+#include "fft_config.h"
+#include "fft_device.cuh"
+#include "glsfft_internal.h"
+
+namespace glsfft {
+
+// Shared-memory accessor for a row line: one padding slot per 16 complex
+// values keeps the stride-R butterfly writes of the first exchange on
+// distinct banks.
+struct RowSm {
+    float2 *base;
+    __device__ __forceinline__ float2 &operator()(int pos) const { return base[pos + (pos >> 4)]; }
+};
+// Column tiles keep [position][column] order (like the image) with the same
+// per-16 padding over the linearised index.
+template <int W>
+struct ColSm {
+    float2 *base;
+    int c;
+    __device__ __forceinline__ float2 &operator()(int pos) const {
+        const int i = pos * W + c;
+        return base[i + (i >> 4)];
+    }
+};
+
+// ------------------------------------------------------------ load / store
+template <int LD>
+__device__ __forceinline__ float2 load_elem(const void *img, const float *win, size_t idx) {
+    if constexpr (LD == LD_C2) {
+        return __ldg(reinterpret_cast<const float2 *>(img) + idx);
+    } else if constexpr (LD == LD_R1) {
+        return make_float2(__ldg(reinterpret_cast<const float *>(img) + idx), 0.0f);
+    } else {  // LD_R1W: window * image, glsBasicOperation.cpp:169
+        return make_float2(__ldg(win + idx) * __ldg(reinterpret_cast<const float *>(img) + idx),
+                           0.0f);
+    }
+}
+
+// ------------------------------------------------------------- row pass
+// Block: LINES rows x T threads.  blockIdx.y selects image 0 or 1.
+template <int N, int E, int LINES, int LD, int ST>
+__global__ void __launch_bounds__(LINES *LineFft<N, E>::T)
+    fft_rows_kernel(PassArgs a) {
+    using F = LineFft<N, E>;
+    constexpr int T = F::T;
+    extern __shared__ float4 smem_raw[];
+    float2 *smem = reinterpret_cast<float2 *>(smem_raw);
+    __shared__ unsigned long long red[(LINES * T + 31) / 32];
+
+    const int l = threadIdx.x / T, t = threadIdx.x % T;
+    const int row = blockIdx.x * LINES + l;
+    const bool active = row < a.rows;
+    const void *in = blockIdx.y ? a.in1 : a.in0;
+    void *out = blockIdx.y ? a.out1 : a.out0;
+    const bool conj_in = a.flags & PF_CONJ_IN;
+
+    float2 x[E];
+#pragma unroll
+    for (int m = 0; m < E; m++) {
+        const int pos = t + m * T;
+        float2 v = active ? load_elem<LD>(in, a.window, (size_t)row * N + pos) : make_float2(0.f, 0.f);
+        x[m] = conj_in ? cconj(v) : v;
+    }
+    F::run(x, t, RowSm{smem + l * padded_count(N)}, a.tw);
+
+    const int orow = (a.flags & PF_SHIFT_ROWS) ? (row + (a.rows >> 1)) & (a.rows - 1) : row;
+    const bool conj_out = a.flags & PF_CONJ_OUT;
+    unsigned long long best = 0;
+#pragma unroll
+    for (int m = 0; m < E; m++) {
+        const int pos = t + m * T;
+        const int ocol = (a.flags & PF_SHIFT_COLS) ? (pos + (N >> 1)) & (N - 1) : pos;
+        float2 v = cscale(x[m], a.scale);
+        if (conj_out) v = cconj(v);
+        const size_t o = (size_t)orow * N + ocol;
+        if constexpr (ST == ST_C2) {
+            if (active) reinterpret_cast<float2 *>(out)[o] = v;
+        } else {
+            if (active) reinterpret_cast<float *>(out)[o] = v.x;
+            if constexpr (ST == ST_RE_ARGMAX) {
+                unsigned long long k = active ? argmax_key(v.x, (unsigned)o) : 0ull;
+                best = k > best ? k : best;
+            }
+        }
+    }
+    if constexpr (ST == ST_RE_ARGMAX) block_argmax_commit(best, red, a.key);
+}
+
+// ---------------------------------------------------------- column pass
+// Block: W adjacent columns x T threads, column index fastest.
+template <int N, int E, int W, int LD, int ST>
+__global__ void __launch_bounds__(W *LineFft<N, E>::T)
+    fft_cols_kernel(PassArgs a) {
+    using F = LineFft<N, E>;
+    constexpr int T = F::T;
+    extern __shared__ float4 smem_raw[];
+    float2 *smem = reinterpret_cast<float2 *>(smem_raw);
+
+    const int c = threadIdx.x % W, t = threadIdx.x / W;
+    const int col = blockIdx.x * W + c;
+    const int cols = a.cols;
+    const bool active = col < cols;
+    const void *in = blockIdx.y ? a.in1 : a.in0;
+    void *out = blockIdx.y ? a.out1 : a.out0;
+    const bool conj_in = a.flags & PF_CONJ_IN;
+
+    float2 x[E];
+#pragma unroll
+    for (int m = 0; m < E; m++) {
+        const int pos = t + m * T;
+        float2 v = active ? load_elem<LD>(in, a.window, (size_t)pos * cols + col) : make_float2(0.f, 0.f);
+        x[m] = conj_in ? cconj(v) : v;
+    }
+    F::run(x, t, ColSm<W>{smem, c}, a.tw);
+
+    const int ocol = (a.flags & PF_SHIFT_COLS) ? (col + (cols >> 1)) & (cols - 1) : col;
+    const bool conj_out = a.flags & PF_CONJ_OUT;
+#pragma unroll
+    for (int m = 0; m < E; m++) {
+        const int pos = t + m * T;
+        const int orow = (a.flags & PF_SHIFT_ROWS) ? (pos + (N >> 1)) & (N - 1) : pos;
+        float2 v = cscale(x[m], a.scale);
+        if (conj_out) v = cconj(v);
+        const size_t o = (size_t)orow * cols + ocol;
+        if constexpr (ST == ST_C2) {
+            if (active) reinterpret_cast<float2 *>(out)[o] = v;
+        } else {
+            if (active) reinterpret_cast<float *>(out)[o] = v.x;
+        }
+    }
+}
+
+// --------------------------------------------- fused phaseCorrelate columns
+// in0 = row-pass output of src1 (or, with PF_F1_SPECTRUM, its resident full
+// 2-D spectrum), in1 = row-pass output of src2.  Each block finishes the
+// forward column FFTs of both, forms the phase-only cross spectrum
+// P = F1 conj(F2) / |F1 conj(F2)| (glsBasicOperation.cpp:195-206) and runs
+// the column FFT of conj(P) -- the first half of the unscaled inverse
+// conj(FFT2(conj P)); the row pass that follows only needs the real part,
+// which the outer conj leaves unchanged.  Writes to out0 (may alias in0).
+// |t| = 0 gives P = 0 (the reference divides 0/0 into NaN).
+template <int N, int E, int W>
+__global__ void __launch_bounds__(W *LineFft<N, E>::T)
+    poc_cols_kernel(PassArgs a) {
+    using F = LineFft<N, E>;
+    constexpr int T = F::T;
+    extern __shared__ float4 smem_raw[];
+    float2 *smem = reinterpret_cast<float2 *>(smem_raw);
+
+    const int c = threadIdx.x % W, t = threadIdx.x / W;
+    const int col = blockIdx.x * W + c;
+    const int cols = a.cols;
+    const bool active = col < cols;
+    const float2 *f1 = reinterpret_cast<const float2 *>(a.in0);
+    const float2 *f2 = reinterpret_cast<const float2 *>(a.in1);
+    ColSm<W> sm{smem, c};
+
+    float2 x[E], y[E];
+#pragma unroll
+    for (int m = 0; m < E; m++) {
+        const size_t i = (size_t)(t + m * T) * cols + col;
+        y[m] = active ? __ldg(f2 + i) : make_float2(0.f, 0.f);
+    }
+    F::run(y, t, sm, a.tw);
+#pragma unroll
+    for (int m = 0; m < E; m++) {
+        const size_t i = (size_t)(t + m * T) * cols + col;
+        x[m] = active ? __ldg(f1 + i) : make_float2(0.f, 0.f);
+    }
+    if (!(a.flags & PF_F1_SPECTRUM)) F::run(x, t, sm, a.tw);
+#pragma unroll
+    for (int m = 0; m < E; m++) {
+        const float2 s0 = x[m], s1 = y[m];
+        const float tr = s0.x * s1.x + s0.y * s1.y;
+        const float ti = -s0.x * s1.y + s0.y * s1.x;
+        const float mag = sqrtf(tr * tr + ti * ti);
+        // conj(P): the inverse is taken as conj(FFT(conj P))
+        x[m] = mag > 0.f ? make_float2(tr / mag, -(ti / mag)) : make_float2(0.f, 0.f);
+    }
+    F::run(x, t, sm, a.tw);
+    float2 *out = reinterpret_cast<float2 *>(a.out0);
+#pragma unroll
+    for (int m = 0; m < E; m++) {
+        const size_t o = (size_t)(t + m * T) * cols + col;
+        if (active) out[o] = x[m];
+    }
+}
+
+// --------------------------------------------------- centroid finish
+// One thread: decode the argmax key, FP64 weighted centroid over the clamped
+// box in row-major order (glsPhaseCorrelate.cpp:60-137), response divided by
+// rows*cols (:224-225), shift = center - centroid (:228-230).
+// res[0..2] = dx, dy, response; res[3] = peak index as a double, res[4] = peak value.
+__global__ void poc_finish_kernel(const float *surface, int rows, int cols, int box,
+                                  const unsigned long long *key, double *res);
+
+}  // namespace glsfft

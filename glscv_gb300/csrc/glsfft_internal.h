@@ -1,0 +1,51 @@
+// glsfft_internal.h -- shared declarations between the C ABI and the kernel
+// translation units.  Not a public header.
+#pragma once
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+namespace glsfft {
+
+constexpr int kMaxLen = 4096;  // largest supported FFT length per dimension
+
+// load modes of the first pass
+enum { LD_C2 = 0, LD_R1 = 1, LD_R1W = 2 };
+// store modes of the last pass
+enum { ST_C2 = 0, ST_RE = 1, ST_RE_ARGMAX = 2 };
+// per-pass flags
+enum : unsigned {
+    PF_CONJ_IN = 1u << 0,
+    PF_CONJ_OUT = 1u << 1,
+    PF_SHIFT_ROWS = 1u << 2,
+    PF_SHIFT_COLS = 1u << 3,
+    PF_F1_SPECTRUM = 1u << 4,
+};
+
+struct PassArgs {
+    const void *in0;
+    const void *in1;
+    void *out0;
+    void *out1;
+    const float *window;
+    int rows, cols;
+    float scale;
+    unsigned flags;
+    unsigned long long *key;
+    const float2 *tw;  // twiddle table of this pass's length
+};
+
+// Launchers (fft_rows.cu, fft_cols.cu, poc.cu).  They return cudaSuccess or
+// the launch error; `images` is 1 or 2 (blockIdx.y selects in0/in1).
+cudaError_t launch_rows(int n, int ld, int st, const PassArgs &a, int images, cudaStream_t s);
+cudaError_t launch_cols(int n, int ld, int st, const PassArgs &a, int images, cudaStream_t s);
+cudaError_t launch_poc_cols(int n, const PassArgs &a, cudaStream_t s);
+cudaError_t launch_poc_finish(const float *surface, int rows, int cols, int box,
+                              const unsigned long long *key, double *res, cudaStream_t s);
+
+// Twiddle tables: one device buffer, table for length n (power of two,
+// 2 <= n <= kMaxLen) at entries [n, 2n), value e^{-2 pi i k/n}.  Generated in
+// FP64 on the host and rounded once to FP32.
+void make_twiddle_host(float2 *dst /* 2*kMaxLen entries */);
+
+}  // namespace glsfft

@@ -1,0 +1,134 @@
+/*
+ * glsfft.h -- C ABI of the GB300 FFT / phaseCorrelate path of glsCV.
+ *
+ * Plain C: opaque handles, int status codes (0 = success), device pointers,
+ * and `void *stream` (a cudaStream_t; NULL = the legacy default stream).
+ * Every call validates its arguments on the host before any launch and
+ * returns a status instead of throwing; the C++ layer in <gls/glsCV.h>
+ * turns a non-zero status into a gls::Exception, as the reference's
+ * GLS_Assert/CV_Assert throws cv::Exception (glsCV/glsMacro.h:40).
+ *
+ * Image layout: row-major, continuous, like a continuous cv::Mat.
+ * CV_32FC2 = interleaved float (re, im), 8 bytes per pixel, 8-byte aligned;
+ * CV_32FC1 = float, 4-byte aligned.  rows and cols are powers of two in
+ * [1, GLSFFT_MAX_LEN]; square, rectangular and 1-D (1 x N, N x 1) shapes are
+ * all accepted (the reference asserts on non-square 2-D, glsFft.cpp:503-517).
+ *
+ * Threading: a context may be used from one host thread at a time; calls on
+ * one context share its workspace, so issue them on one stream (or
+ * synchronise between streams).  Separate contexts are independent.
+ */
+#ifndef GLSFFT_H_
+#define GLSFFT_H_
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define GLSFFT_API __attribute__((visibility("default")))
+#else
+#define GLSFFT_API
+#endif
+
+#define GLSFFT_MAX_LEN 4096
+
+/* Flag bits: the reference's values (glsCV/glsFft.h:43-47, OpenCV DFT_*). */
+#define GLSFFT_INVERSE 1 /* GLS_FFT_INVERSE = DFT_INVERSE */
+#define GLSFFT_SCALE 2   /* GLS_FFT_SCALE = DFT_SCALE: x 1/N per dimension */
+#define GLSFFT_SHIFT 64  /* GLS_FFT_SHIFT: quadrant swap of the output */
+
+enum glsfft_status {
+    GLSFFT_SUCCESS = 0,
+    GLSFFT_ERROR_INVALID_VALUE = 1, /* NULL pointer or handle, unknown flag bit, bad box */
+    GLSFFT_ERROR_NOT_POW2 = 2,      /* GLS_Assert(IsPow2(N)), glsFft.cpp:681 */
+    GLSFFT_ERROR_SIZE = 3,          /* a dimension outside [1, GLSFFT_MAX_LEN] */
+    GLSFFT_ERROR_MISALIGNED = 4,    /* pointer not aligned to its element size */
+    GLSFFT_ERROR_CUDA = 5,          /* a CUDA runtime call or launch failed */
+    GLSFFT_ERROR_OUT_OF_MEMORY = 6, /* device workspace allocation failed */
+    GLSFFT_ERROR_BUDGET = 7,        /* workspace would exceed the context's HBM budget */
+    GLSFFT_ERROR_TIMEOUT = 8,       /* a bounded device-side wait expired */
+    GLSFFT_ERROR_SHAPE = 9          /* inputs of different shapes */
+};
+
+typedef struct glsfft_context_s *glsfft_context;
+
+/* Human-readable text for a status code (never NULL). */
+GLSFFT_API const char *glsfft_status_string(int status);
+
+/* Library version as MAJOR*10000 + MINOR*100 + PATCH. */
+GLSFFT_API int glsfft_version(void);
+
+/*
+ * Create a context on CUDA device `device`: uploads the FP32 twiddle tables
+ * (generated in FP64, once) for every length up to GLSFFT_MAX_LEN.
+ * Replaces glsCvInit() (glsCV/glsCV.cpp:89-165): no GL context, no window.
+ */
+GLSFFT_API int glsfft_context_create(glsfft_context *ctx, int device);
+
+/* Free the context and its workspace.  Replaces glsCvTerminate(). */
+GLSFFT_API int glsfft_context_destroy(glsfft_context ctx);
+
+/* Cap the workspace the context may hold on the device (bytes; 0 = none). */
+GLSFFT_API int glsfft_context_set_budget(glsfft_context ctx, size_t bytes);
+
+/* Bytes of device workspace the context currently holds. */
+GLSFFT_API int glsfft_context_workspace(glsfft_context ctx, size_t *bytes);
+
+/*
+ * 2-D complex FFT of a CV_32FC2 rows x cols device image:
+ * gls::fft(src, dst, flag), glsCV/glsFft.h:55 / glsFft.cpp:675-708.
+ * Rows pass then columns pass, one kernel each.  src == dst is allowed
+ * (in-place, as glsPhaseCorrelate.cpp:199 uses it).  Asynchronous on
+ * `stream`; uses no workspace.
+ */
+GLSFFT_API int glsfft_fft2d_c2c(glsfft_context ctx, const void *src, void *dst, int rows,
+                                int cols, int flags, void *stream);
+
+/*
+ * Same for a CV_32FC1 src promoted to complex with imag = 0
+ * (gls::fft's merge step, glsFft.cpp:684-689); dst is CV_32FC2.
+ */
+GLSFFT_API int glsfft_fft2d_r2c_promote(glsfft_context ctx, const float *src, void *dst,
+                                        int rows, int cols, int flags, void *stream);
+
+/*
+ * gls::phaseCorrelate(src1, src2, window, &response),
+ * glsCV/glsPhaseCorrelate.h:58 / glsPhaseCorrelate.cpp:142-236.
+ * src1, src2: CV_32FC1 rows x cols device images; window: same shape or
+ * NULL.  box: centroid box edge (the reference uses 5, glsPhaseCorrelate.cpp:219).
+ * Writes the shift of src2 relative to src1 and the response
+ * (sum over the box / (rows*cols)); dx/dy/response are host pointers
+ * (response may be NULL).  Synchronises `stream`.  Uses the context workspace
+ * (20 * rows * cols bytes).
+ */
+GLSFFT_API int glsfft_phase_correlate(glsfft_context ctx, const float *src1, const float *src2,
+                                      const float *window, int rows, int cols, int box,
+                                      double *dx, double *dy, double *response, void *stream);
+
+/*
+ * Asynchronous form: writes 5 doubles to device memory `d_result`
+ * {dx, dy, response, peak row-major index, peak value}; nothing is copied
+ * to the host and nothing synchronises.
+ */
+GLSFFT_API int glsfft_phase_correlate_async(glsfft_context ctx, const float *src1,
+                                            const float *src2, const float *window, int rows,
+                                            int cols, int box, double *d_result, void *stream);
+
+/*
+ * Copy the real, quadrant-swapped correlation surface of the last
+ * phaseCorrelate on this context (the plane the reference downloads for its
+ * centroid, glsPhaseCorrelate.cpp:219) into the device buffer `dst` of
+ * `count` floats (count must equal rows*cols of that call).  Asynchronous
+ * on `stream`.  For tests and debugging.
+ */
+GLSFFT_API int glsfft_phase_correlate_surface(glsfft_context ctx, float *dst, size_t count,
+                                              void *stream);
+
+#ifdef __cplusplus
+} /* extern "C" */
+#endif
+
+#endif /* GLSFFT_H_ */

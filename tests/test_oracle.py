@@ -1,0 +1,134 @@
+"""The oracle pinned against the reference (CPU only).
+
+* bit-exact against tests/golden/fft_golden.npz, which the reference's own
+  fft_stockhum.cpp produced (tests/golden/make_golden.py);
+* bit-exact against the reference compiled here (oracle/_ref), where built;
+* within FP32 accuracy of an FP64 DFT at every size;
+* phaseCorrelate restatement recovers known shifts; first-occurrence argmax.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from glscv_gb300 import workloads as wl
+
+
+def _cases(golden):
+    return sorted({k.split("__")[0] for k in golden.files})
+
+
+def test_port_matches_reference_golden_vectors(oracle, golden):
+    for name in _cases(golden):
+        rows, cols, flags, seed, algo = (int(v) for v in golden[f"{name}__meta"])
+        x = golden[f"{name}__in"]
+        np.testing.assert_array_equal(x, wl.complex_uniform(rows, cols, seed))
+        y = oracle.fft2d(x, flags, algo)
+        ref = golden[f"{name}__out"]
+        assert np.array_equal(y.view(np.uint32), ref.view(np.uint32)), name
+
+
+def test_golden_passes_reference_tolerance_vs_fp64(oracle, golden):
+    """The reference test's criterion (ULPS 64, EPS 1e-6*N unless SCALE,
+    unittest_glsFft.cpp:101-105) holds for the golden outputs vs FP64."""
+    for name in _cases(golden):
+        rows, cols, flags, seed, algo = (int(v) for v in golden[f"{name}__meta"])
+        x = golden[f"{name}__in"]
+        ref64 = oracle.fft2d_f64(x, flags).astype(np.complex64)
+        n = max(rows, cols)
+        assert oracle.are_equal(ref64, golden[f"{name}__out"], 64, oracle.fft_eps(n, flags)) == 0, name
+
+
+def test_port_matches_reference_build_bit_exact(oracle):
+    if oracle.ref_lib() is None:
+        oracle.build_ref()
+    if oracle.ref_lib() is None:
+        pytest.skip("reference checkout not present: oracle/_ref not built")
+    for n in (2, 4, 8, 64, 128, 512):
+        x = wl.complex_uniform(n, n, 1000 + n)
+        a = oracle.fft_r2t1_square(x)
+        b = oracle.ref_fft_r2t1_square(x)
+        assert np.array_equal(a.view(np.uint32), b.view(np.uint32)), n
+    for shape in ((4, 4), (8, 32), (256, 16), (1, 64), (128, 1), (1024, 2048)):
+        x = wl.complex_uniform(*shape, 7)
+        a = oracle.fft2d(x, 0, 1)
+        b = oracle.ref_fft_r4_lines(x)
+        assert np.array_equal(a.view(np.uint32), b.view(np.uint32)), shape
+
+
+def test_planted_error_is_caught(oracle, golden):
+    """A one-ULP change in one oracle output element fails the bit-exact pin."""
+    x = golden["FFT_16x16__in"]
+    y = oracle.fft2d(x, 0, 0)
+    bad = y.copy().view(np.uint32)
+    bad[3, 5] += 1
+    assert not np.array_equal(bad, golden["FFT_16x16__out"].view(np.uint32))
+
+
+@pytest.mark.parametrize("n", [2, 4, 16, 128, 1024])
+def test_port_accuracy_vs_fp64(oracle, n):
+    x = wl.complex_uniform(n, n, n)
+    for algo in (0, 1):
+        for flags in (0, oracle.DFT_INVERSE | oracle.DFT_SCALE, oracle.GLS_FFT_SHIFT):
+            y = oracle.fft2d(x, flags, algo)
+            assert oracle.rel_l2(y, oracle.fft2d_f64(x, flags)) < 1e-6
+
+
+def test_round_trip(oracle):
+    x = wl.complex_uniform(256, 256, 0)
+    y = oracle.fft2d(oracle.fft2d(x, 0), oracle.DFT_INVERSE | oracle.DFT_SCALE)
+    assert oracle.rel_l2(y, x) < 1e-6
+
+
+def test_max_loc_first_occurrence(oracle):
+    c = np.zeros((8, 8), np.float32)
+    c[2, 5] = 3.0
+    c[6, 1] = 3.0
+    c[0, 0] = np.nan
+    (px, py), v = oracle.max_loc(c)
+    assert (px, py) == (5, 2) and v == 3.0
+    c2 = np.full((4, 4), np.nan, np.float32)
+    assert oracle.max_loc(c2)[0] == (0, 0)
+
+
+@pytest.mark.parametrize("n", [32, 64, 256])
+def test_phase_correlate_restatement_recovers_integer_shift(oracle, n):
+    """White-spectrum input (the reference test's uniform image), integer shift."""
+    dx, dy = n // 8 - 1, -(n // 16) + 2
+    a, b = wl.random_pair(n, n, seed=n, shift=(dx, dy))
+    for win in (None, wl.hann_window(n, n)):
+        (mx, my), resp, peak, _ = oracle.phase_correlate(a, b, win, box=5)
+        assert peak == (n // 2 - dx, n // 2 - dy)
+        assert abs(mx - dx) < 0.25 and abs(my - dy) < 0.25
+        assert 0.0 < resp <= 1.5
+
+
+def test_phase_correlate_restatement_subpixel(oracle):
+    n = 128
+    a, b = wl.random_pair(n, n, seed=5, shift=(7.3, -4.4))
+    (mx, my), resp, _, _ = oracle.phase_correlate(a, b, wl.hann_window(n, n), box=5)
+    # the reference test's bar is "within 0.25 px of what OpenCV gets"
+    # (UnitTest_glsPhaseCorrelate.cpp:129-132); the 5x5 centroid is biased
+    # toward the integer peak, so allow that bias here
+    assert abs(mx - 7.3) < 0.35 and abs(my + 4.4) < 0.45
+
+
+@pytest.mark.parametrize("n", [128, 256])
+def test_phase_correlate_smooth_field_reference_nan_and_guard(oracle, n):
+    """Config-2b style smooth field: its FP32 spectrum has exactly-zero bins,
+    so the reference's epsilon-free phase-only step (glsBasicOperation.cpp:
+    202-205) turns the whole surface into NaN; with the zero guard (|t| = 0
+    -> 0, the GB300 path's behaviour) the integer shift is found exactly."""
+    a, b, (dx, dy) = wl.shifted_pair(n, n, seed_field=6, seed_shift=7, max_shift=n // 8)
+    win = wl.hann_window(n, n)
+    (rx, ry), _, _, _ = oracle.phase_correlate(a, b, win, zero_guard=False)
+    (gx, gy), resp, peak, _ = oracle.phase_correlate(a, b, win, zero_guard=True)
+    assert peak == (n // 2 - dx, n // 2 - dy)
+    assert abs(gx - dx) < 0.25 and abs(gy - dy) < 0.25
+    assert np.isnan(rx) or abs(rx - dx) < 0.25  # NaN whenever a zero bin occurs
+
+
+def test_hann_window_shape():
+    w = wl.hann_window(8, 16)
+    assert w.shape == (8, 16) and w.dtype == np.float32
+    assert w[0, 0] == 0.0 and abs(w[4, 8] - np.sin(np.pi * 4 / 7) ** 2 * np.sin(np.pi * 8 / 15) ** 2) < 1e-6

@@ -1,0 +1,117 @@
+"""gls::phaseCorrelate on the GPU through the C ABI, against the oracle.
+
+* White-spectrum inputs (the reference test's uniform images,
+  UnitTest_glsPhaseCorrelate.cpp:87): integer peak identical to the oracle's,
+  sub-pixel shift within 1e-3 px of the oracle, response within 1e-4.
+* Smooth-field inputs (Gaussian-blurred noise): bins where src1 carries no
+  energy hold FP32 rounding noise, which the phase-only normalisation lifts
+  to unit magnitude with an implementation-specific phase; the integer peak
+  is still identical and must equal the true shift, while the sub-pixel
+  value is compared with a 0.05 px tolerance.
+* The ground truth (the synthetic shift) is met within the reference test's
+  0.25 px (UnitTest_glsPhaseCorrelate.cpp:128-132).
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from glscv_gb300 import workloads as wl
+from tests.gpu_util import gpu_phase_correlate
+
+pytestmark = pytest.mark.gpu
+
+
+def _peak(n_rows, n_cols, dx, dy):
+    return (int(round(n_cols / 2 - dx)) % n_cols, int(round(n_rows / 2 - dy)) % n_rows)
+
+
+@pytest.mark.parametrize("shape", [(32, 32), (64, 64), (256, 256), (1024, 1024), (64, 128),
+                                   (512, 256), (2048, 2048)])
+def test_white_spectrum_integer_shift(ctx, torch_cuda, oracle, shape):
+    rows, cols = shape
+    dx, dy = cols // 8 - 3, -(rows // 16) + 1
+    a, b = wl.random_pair(rows, cols, seed=rows + cols, shift=(dx, dy))
+    win = wl.hann_window(rows, cols)
+    for w in (win, None):
+        (ox, oy), oresp, opeak, osurf = oracle.phase_correlate(a, b, w, box=5, want_surface=True)
+        (gx, gy), gresp, gsurf = gpu_phase_correlate(ctx, torch_cuda, a, b, w, box=5,
+                                                     want_surface=True)
+        (px, py), _ = oracle.max_loc(gsurf)
+        assert (px, py) == opeak == _peak(rows, cols, dx, dy)
+        assert abs(gx - ox) < 1e-3 and abs(gy - oy) < 1e-3
+        assert abs(gresp - oresp) < 1e-4
+        assert abs(gx - dx) < 0.25 and abs(gy - dy) < 0.25
+        assert oracle.rel_l2(gsurf, osurf) < 1e-3
+
+
+@pytest.mark.parametrize("box", [1, 3, 5, 7])
+def test_subpixel_and_box(ctx, torch_cuda, oracle, box):
+    n = 256
+    a, b = wl.random_pair(n, n, seed=21, shift=(10.37, -5.62))
+    win = wl.hann_window(n, n)
+    (ox, oy), oresp, _, _ = oracle.phase_correlate(a, b, win, box=box)
+    (gx, gy), gresp, _ = gpu_phase_correlate(ctx, torch_cuda, a, b, win, box=box)
+    assert abs(gx - ox) < 1e-3 and abs(gy - oy) < 1e-3
+    assert abs(gresp - oresp) < 1e-4
+
+
+@pytest.mark.parametrize("n,max_shift", [(512, 50), (1024, 100), (2048, 100)])
+def test_smooth_field_config2b(ctx, torch_cuda, oracle, n, max_shift):
+    """A = blurred noise (sigma 4 px) in [0,1], B = A rolled by an integer
+    shift in [-max_shift, max_shift] + N(0, 0.01^2), Hann window (1024 with
+    +-100 px is the benchmark workload; the shift range scales with n because
+    a Hann-windowed smooth field loses its peak once the shift nears n/2)."""
+    a, b, (dx, dy) = wl.shifted_pair(n, n, seed_field=6, seed_shift=7, max_shift=max_shift)
+    win = wl.hann_window(n, n)
+    (ox, oy), oresp, opeak, _ = oracle.phase_correlate(a, b, win, box=5)
+    (gx, gy), gresp, gsurf = gpu_phase_correlate(ctx, torch_cuda, a, b, win, box=5,
+                                                 want_surface=True)
+    (px, py), _ = oracle.max_loc(gsurf)
+    assert (px, py) == opeak == _peak(n, n, dx, dy)
+    assert abs(gx - ox) < 0.05 and abs(gy - oy) < 0.05
+    assert abs(gx - dx) < 0.25 and abs(gy - dy) < 0.25
+
+
+def test_identical_images_zero_shift(ctx, torch_cuda):
+    n = 128
+    a = np.random.default_rng(3).uniform(0, 1, (n, n)).astype(np.float32)
+    (gx, gy), resp, _ = gpu_phase_correlate(ctx, torch_cuda, a, a, wl.hann_window(n, n))
+    assert abs(gx) < 1e-6 and abs(gy) < 1e-6
+    assert 0.5 < resp < 1.5
+
+
+def test_constant_image_zero_bins_are_finite(ctx, torch_cuda):
+    """All-zero cross spectrum except DC: the reference would produce NaN
+    (0/0, glsBasicOperation.cpp:202-205); the GB300 path maps |t| = 0 to 0."""
+    n = 64
+    a = np.full((n, n), 0.5, np.float32)
+    (gx, gy), resp, _ = gpu_phase_correlate(ctx, torch_cuda, a, a, None)
+    assert np.isfinite(gx) and np.isfinite(gy) and np.isfinite(resp)
+
+
+def test_async_matches_sync(ctx, torch_cuda, oracle):
+    torch = torch_cuda
+    n = 512
+    a, b = wl.random_pair(n, n, seed=9, shift=(-33, 17))
+    win = wl.hann_window(n, n)
+    (gx, gy), gresp, _ = gpu_phase_correlate(ctx, torch, a, b, win)
+    da, db, dw = (torch.from_numpy(v).cuda() for v in (a, b, win))
+    res = torch.zeros(8, dtype=torch.float64, device="cuda")
+    ctx.phase_correlate_async(da.data_ptr(), db.data_ptr(), dw.data_ptr(), n, n, 5,
+                              res.data_ptr(), torch.cuda.current_stream().cuda_stream)
+    r = res.cpu().numpy()
+    assert r[0] == gx and r[1] == gy and r[2] == gresp
+    assert int(r[3]) == (n // 2 - 17) * n + (n // 2 + 33)
+
+
+def test_budget_error(native, torch_cuda):
+    import glscv_gb300 as g
+    torch = torch_cuda
+    with g.Context(0) as c:
+        c.set_budget(1024)
+        d = torch.zeros((64, 64), dtype=torch.float32, device="cuda")
+        with pytest.raises(g.GlsError) as e:
+            c.phase_correlate(d.data_ptr(), d.data_ptr(), None, 64, 64)
+        assert e.value.status == 7
+        assert c.workspace_bytes() == 0
