@@ -1,0 +1,391 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 FFT / phaseCorrelate path (one JSON line on rank 0).
+
+Workload (one step): a batch of 1024x1024 CV_32FC2 images, each transformed
+forward and back (INVERSE|SCALE) by gls::fft -- the 2-D FFT of the plain
+single-image configuration, over a batch large enough (64 images, 512 MiB)
+that inputs exceed the 129 MB L2, so no flush is needed between steps.
+Metric: GFLOP/s in the 5 N log2 N convention (N = rows*cols per 2-D FFT).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl own|reference]
+
+Multi-GPU: the path shards by image with no exchange, so each rank runs its
+own batch (weak scaling, replicas); value = all ranks' work / max rank time.
+`--impl reference` times the reference's CPU Stockham (fft_stockhum.cpp
+radix-2 type1, compiled from the reference where that build exists, else its
+restatement in oracle/) on all host cores, rank 0 only.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "2D FFT GFLOP/s batched+TC vs plain FP32 @relL2<=1e-5 vs FP64; PC p99 ms"
+UNIT = "GFLOP/s"
+ROWS = COLS = 1024
+INV, SCALE = 1, 2
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=["own", "reference"], default="own")
+    p.add_argument("--images", type=int, default=64, help="images per step per GPU")
+    p.add_argument("--cpu-sample", type=int, default=2, help="images per CPU-baseline step")
+    p.add_argument("--no-e2e", action="store_true")
+    return p.parse_args()
+
+
+def flops_per_image() -> float:
+    n = ROWS * COLS
+    return 2 * 5.0 * n * math.log2(n)  # forward + inverse
+
+
+def config(images: int, n_gpus: int) -> dict:
+    return {
+        "workload": f"gls::fft 2-D complex {ROWS}x{COLS} CV_32FC2, forward + inverse(SCALE), "
+                    f"{images} images per GPU per step",
+        "rows": ROWS, "cols": COLS, "images_per_gpu": images, "global_images": images * n_gpus,
+        "input": "uniform[-1,1) complex, seeded (numpy PCG64)",
+        "l2": f"inputs {images * ROWS * COLS * 8 >> 20} MiB per GPU > 129 MB L2; no flush",
+        "parallelism": f"replicas x{n_gpus} (images sharded, no collective)",
+    }
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    """nvidia-smi samples during the timed region (clocks + throttle reasons)."""
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "100", "-i", str(self.index)],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+            out, _ = self.proc.communicate()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.strip().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[0]))
+                smax.append(float(f[1]))
+            except ValueError:
+                continue
+            for name, v in zip(names, f[4:8]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def measured_peaks() -> tuple[float, str]:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            return float(json.loads(p.read_text())["hbm_gbs"]), "measured"
+        except Exception:
+            pass
+    return 6800.0, "fallback"
+
+
+def traffic_per_launch(kernel: str):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary."""
+    f = ROOT / "profiles" / "traffic_per_launch.txt"
+    if not f.exists():
+        return None
+    for line in f.read_text().splitlines():
+        parts = line.split()
+        if len(parts) >= 2 and parts[0] == kernel:
+            try:
+                return float(parts[1])
+            except ValueError:
+                return None
+    return None
+
+
+# -------------------------------------------------------------- CPU baseline
+def cpu_baseline(images: int, steps: int = 1, warmup: int = 0) -> dict:
+    """The reference's CPU Stockham on all host threads over `images` images
+    (forward + inverse each); returns value in GFLOP/s."""
+    import numpy as np
+    from glscv_gb300 import workloads as wl
+    from oracle import oracle as orc
+    orc.build()
+    kind = "port"
+    fwd = orc.fft_r2t1_square
+    if orc.ref_lib() is None and Path("/root/reference/UnitTest_glsCV/fft_stockhum.cpp").exists():
+        try:
+            orc.build_ref()
+        except Exception:
+            pass
+    if orc.ref_lib() is not None:
+        kind, fwd = "reference", orc.ref_fft_r2t1_square
+    threads = os.cpu_count() or 1
+    orc.set_threads(threads)
+    xs = [wl.complex_uniform(ROWS, COLS, 5000 + i) for i in range(images)]
+
+    def one_step():
+        for x in xs:
+            f = fwd(x)
+            # inverse = conj(F(conj y)) / N, composed as gls::fft defines it
+            y = np.conj(fwd(np.conj(f).astype(np.complex64))) / np.float32(ROWS * COLS)
+        return y
+
+    for _ in range(warmup):
+        one_step()
+    t = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        one_step()
+        t.append(time.perf_counter() - t0)
+    sec = statistics.median(t)
+    value = images * flops_per_image() / sec / 1e9
+    return {"value": round(value, 3), "unit": UNIT, "cores": orc.num_threads(), "kind": kind,
+            "sample": f"{images} x {ROWS}x{COLS} images forward+inverse per step "
+                      f"(fft_dit_Stockham_radix2_type1), median of {steps} step(s), "
+                      f"{sec * 1e3:.1f} ms per step"}
+
+
+def run_reference(args) -> None:
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    n_gpus = args.gpus
+    cb = cpu_baseline(args.cpu_sample, steps=max(1, args.steps), warmup=max(0, min(args.warmup, 1)))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT,
+        "n_gpus": n_gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(args.cpu_sample * flops_per_image() / (cb["value"] * 1e9) * 1e3, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic", "config": config(args.images, n_gpus),
+        "cpu_baseline": cb,
+        "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+        "note": "reference GPU path is OpenGL 3.3 fragment shaders: unavailable on this box; "
+                "the reference's own CPU Stockham is timed instead",
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------- own arm
+def run_own(args) -> None:
+    import numpy as np
+    import torch
+
+    import glscv_gb300 as g
+    from glscv_gb300 import workloads as wl
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    def max_over_ranks(v: float) -> float:
+        if dist is None:
+            return v
+        t = torch.tensor([v], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    B = args.images
+    ctx = g.Context(local)
+    stream = torch.cuda.current_stream()
+    s = stream.cuda_stream
+    host = torch.empty((B, ROWS, COLS), dtype=torch.complex64).pin_memory()
+    for i in range(B):
+        host[i] = torch.from_numpy(wl.complex_uniform(ROWS, COLS, 1000 + rank * B + i))
+    d_in = host.to("cuda", non_blocking=False)
+    d_out = torch.empty_like(d_in)
+    ptr_in = [d_in[i].data_ptr() for i in range(B)]
+    ptr_out = [d_out[i].data_ptr() for i in range(B)]
+
+    launches_per_step = 4 * B
+    ev = {}
+
+    def step(record: bool):
+        # forward rows, forward cols, inverse rows, inverse cols (+SCALE):
+        # the two passes of gls::fft twice, timed per kernel
+        for i in range(B):
+            for kind, fn, src, flags in (("rows", ctx.fft_rows, ptr_in[i], 0),
+                                         ("cols", ctx.fft_cols, ptr_out[i], 0),
+                                         ("rows", ctx.fft_rows, ptr_out[i], INV),
+                                         ("cols", ctx.fft_cols, ptr_out[i], INV | SCALE)):
+                if record:
+                    e0 = torch.cuda.Event(enable_timing=True)
+                    e1 = torch.cuda.Event(enable_timing=True)
+                    e0.record(stream)
+                    fn(src, ptr_out[i], ROWS, COLS, flags, s)
+                    e1.record(stream)
+                    ev.setdefault(kind, []).append((e0, e1))
+                else:
+                    fn(src, ptr_out[i], ROWS, COLS, flags, s)
+
+    for _ in range(max(3, args.warmup)):
+        step(False)
+    torch.cuda.synchronize()
+    barrier()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    t0.record(stream)
+    for _ in range(args.steps):
+        step(True)
+    t1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    barrier()
+    ms = t0.elapsed_time(t1) / args.steps
+    ms = max_over_ranks(ms)
+    value = world * B * flops_per_image() / (ms * 1e-3) / 1e9
+
+    # per-kernel durations inside the timed region
+    durs = {k: [a.elapsed_time(b) for a, b in v] for k, v in ev.items()}
+    avg = {k: sum(v) / len(v) for k, v in durs.items()}
+    tot = {k: sum(v) for k, v in durs.items()}
+    dom = max(tot, key=tot.get)
+    alg_bytes = 16.0 * ROWS * COLS  # one read + one write of 8-byte pixels per pass
+    achieved = alg_bytes / (avg[dom] * 1e-3) / 1e9
+    peak, peak_kind = measured_peaks()
+    kernel_name = {"rows": "fft_rows_kernel<1024>", "cols": "fft_cols_kernel<1024>"}[dom]
+    traffic = traffic_per_launch(kernel_name)
+
+    # accuracy of this run's first image vs FP64
+    x0 = host[0].numpy()
+    f64 = np.fft.fft2(x0.astype(np.complex128))
+    ctx.fft2d(ptr_in[0], ptr_out[0], ROWS, COLS, 0, s)
+    torch.cuda.synchronize()
+    fwd = d_out[0].cpu().numpy()
+    rel_fwd = float(np.linalg.norm(fwd - f64) / np.linalg.norm(f64))
+    ctx.fft2d(ptr_out[0], ptr_out[0], ROWS, COLS, INV | SCALE, s)
+    torch.cuda.synchronize()
+    rt = d_out[0].cpu().numpy()
+    rel_rt = float(np.linalg.norm(rt - x0) / np.linalg.norm(x0))
+
+    # end to end through the C ABI: pinned host -> device, fwd + inv, device -> host
+    e2e = None
+    if not args.no_e2e:
+        host_out = torch.empty_like(host).pin_memory()
+
+        def e2e_step():
+            d_in.copy_(host, non_blocking=True)
+            for i in range(B):
+                ctx.fft2d(ptr_in[i], ptr_out[i], ROWS, COLS, 0, s)
+                ctx.fft2d(ptr_out[i], ptr_out[i], ROWS, COLS, INV | SCALE, s)
+            host_out.copy_(d_out, non_blocking=True)
+
+        e2e_step()
+        torch.cuda.synchronize()
+        barrier()
+        k_e2e = max(1, min(args.steps, 5))
+        a0 = torch.cuda.Event(enable_timing=True)
+        a1 = torch.cuda.Event(enable_timing=True)
+        a0.record(stream)
+        for _ in range(k_e2e):
+            e2e_step()
+        a1.record(stream)
+        torch.cuda.synchronize()
+        e_ms = max_over_ranks(a0.elapsed_time(a1) / k_e2e)
+        nbytes = B * ROWS * COLS * 8
+        e2e = {"value": round(world * B * flops_per_image() / (e_ms * 1e-3) / 1e9, 3),
+               "unit": UNIT, "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
+               "ms_per_step": round(e_ms, 4), "steps": k_e2e}
+
+    # phaseCorrelate 1024x1024 latency (sync C-ABI call, host wall clock)
+    pc = None
+    if rank == 0:
+        a, b, _ = wl.shifted_pair(1024, 1024)
+        w = wl.hann_window(1024, 1024)
+        da, db, dw = (torch.from_numpy(v).cuda() for v in (a, b, w))
+        lat = []
+        for it in range(220):
+            tt = time.perf_counter()
+            ctx.phase_correlate(da.data_ptr(), db.data_ptr(), dw.data_ptr(), 1024, 1024, 5, s)
+            if it >= 20:
+                lat.append(time.perf_counter() - tt)
+        lat.sort()
+        pc = {"p50_ms": round(lat[len(lat) // 2] * 1e3, 4),
+              "p99_ms": round(lat[int(len(lat) * 0.99) - 1] * 1e3, 4),
+              "note": "1024x1024 CV_32FC1 pair + Hann window, one call at a time, host wall clock"}
+
+    if rank == 0:
+        cb = cpu_baseline(min(args.cpu_sample, B))
+        line = {
+            "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": round(ms, 4),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "config": config(B, world),
+            "path": "plain per-image launches (rows kernel + columns kernel per transform)",
+            "rel_l2_vs_fp64": {"forward": rel_fwd, "round_trip": rel_rt},
+            "roofline": {"bound": "hbm", "kernel": kernel_name, "achieved": round(achieved, 1),
+                         "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
+                         "peak_kind": peak_kind, "traffic": traffic,
+                         "alg_bytes_per_launch": alg_bytes,
+                         "avg_launch_us": {k: round(v * 1e3, 3) for k, v in avg.items()},
+                         "time_share": {k: round(v / sum(tot.values()), 4) for k, v in tot.items()}},
+            "cpu_baseline": cb,
+            "e2e": e2e,
+            "phase_correlate": pc,
+            "clocks": clk,
+            "gpu_launches": launches_per_step * args.steps,
+        }
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+    ctx.close()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_own(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -42,6 +42,8 @@ _SIGNATURES = {
     "glsfft_context_workspace": (_ip, [_vp, ctypes.POINTER(_sz)]),
     "glsfft_fft2d_c2c": (_ip, [_vp, _vp, _vp, _ip, _ip, _ip, _vp]),
     "glsfft_fft2d_r2c_promote": (_ip, [_vp, _vp, _vp, _ip, _ip, _ip, _vp]),
+    "glsfft_fft_rows": (_ip, [_vp, _vp, _vp, _ip, _ip, _ip, _vp]),
+    "glsfft_fft_cols": (_ip, [_vp, _vp, _vp, _ip, _ip, _ip, _vp]),
     "glsfft_phase_correlate": (_ip, [_vp, _vp, _vp, _vp, _ip, _ip, _ip, _dp, _dp, _dp, _vp]),
     "glsfft_phase_correlate_async": (_ip, [_vp, _vp, _vp, _vp, _ip, _ip, _ip, _vp, _vp]),
     "glsfft_phase_correlate_surface": (_ip, [_vp, _vp, _sz, _vp]),
@@ -112,6 +114,14 @@ class Context:
               stream: int = 0, real_input: bool = False) -> None:
         fn = lib().glsfft_fft2d_r2c_promote if real_input else lib().glsfft_fft2d_c2c
         check(fn(self.handle, src, dst, rows, cols, flags, stream), "fft2d")
+
+    def fft_rows(self, src: int, dst: int, rows: int, cols: int, flags: int = 0,
+                 stream: int = 0) -> None:
+        check(lib().glsfft_fft_rows(self.handle, src, dst, rows, cols, flags, stream), "fft_rows")
+
+    def fft_cols(self, src: int, dst: int, rows: int, cols: int, flags: int = 0,
+                 stream: int = 0) -> None:
+        check(lib().glsfft_fft_cols(self.handle, src, dst, rows, cols, flags, stream), "fft_cols")
 
     # -- gls::phaseCorrelate -------------------------------------------------
     def phase_correlate(self, src1: int, src2: int, window: int | None, rows: int, cols: int,

@@ -301,6 +301,39 @@ int glsfft_fft2d_r2c_promote(glsfft_context ctx, const float *src, void *dst, in
     return fft2d_launch(ctx, src, dst, rows, cols, flags, true, (cudaStream_t)stream);
 }
 
+static int one_pass(glsfft_context ctx, const void *src, void *dst, int rows, int cols,
+                    int flags, bool along_rows, cudaStream_t s) {
+    int st = check_fft_args(src, dst, rows, cols, flags, false);
+    if (st) return st;
+    if (!ctx) return GLSFFT_ERROR_INVALID_VALUE;
+    DeviceGuard g(ctx->device);
+    if (!g.ok()) return GLSFFT_ERROR_CUDA;
+    const bool inv = flags & GLSFFT_INVERSE;
+    const int n = along_rows ? cols : rows;
+    PassArgs a{};
+    a.in0 = src;
+    a.out0 = dst;
+    a.rows = rows;
+    a.cols = cols;
+    a.scale = (flags & GLSFFT_SCALE) ? 1.0f / (float)n : 1.0f;
+    a.flags = (inv ? PF_CONJ_IN | PF_CONJ_OUT : 0u) |
+              ((flags & GLSFFT_SHIFT) ? (along_rows ? PF_SHIFT_COLS : PF_SHIFT_ROWS) : 0u);
+    a.tw = ctx->d_tw + n;
+    cudaError_t e = along_rows ? launch_rows(n, LD_C2, ST_C2, a, 1, s)
+                               : launch_cols(n, LD_C2, ST_C2, a, 1, s);
+    return cuda_status(e);
+}
+
+int glsfft_fft_rows(glsfft_context ctx, const void *src, void *dst, int rows, int cols,
+                    int flags, void *stream) {
+    return one_pass(ctx, src, dst, rows, cols, flags, true, (cudaStream_t)stream);
+}
+
+int glsfft_fft_cols(glsfft_context ctx, const void *src, void *dst, int rows, int cols,
+                    int flags, void *stream) {
+    return one_pass(ctx, src, dst, rows, cols, flags, false, (cudaStream_t)stream);
+}
+
 int glsfft_phase_correlate_async(glsfft_context ctx, const float *src1, const float *src2,
                                  const float *window, int rows, int cols, int box,
                                  double *d_result, void *stream) {

@@ -95,6 +95,19 @@ GLSFFT_API int glsfft_fft2d_r2c_promote(glsfft_context ctx, const float *src, vo
                                         int rows, int cols, int flags, void *stream);
 
 /*
+ * One pass of gls::fft on its own: a 1-D FFT of every row (length cols) --
+ * the rows pass, glsFft.cpp:561-605 -- or of every column (length rows) --
+ * the columns pass, glsFft.cpp:607-652.  INVERSE conjugates input and output
+ * of each line, SCALE multiplies by 1/length, SHIFT swaps the halves of each
+ * line.  fft2d(flags) equals fft_rows then fft_cols with the same flags.
+ * One kernel launch each; src == dst allowed.
+ */
+GLSFFT_API int glsfft_fft_rows(glsfft_context ctx, const void *src, void *dst, int rows,
+                               int cols, int flags, void *stream);
+GLSFFT_API int glsfft_fft_cols(glsfft_context ctx, const void *src, void *dst, int rows,
+                               int cols, int flags, void *stream);
+
+/*
  * gls::phaseCorrelate(src1, src2, window, &response),
  * glsCV/glsPhaseCorrelate.h:58 / glsPhaseCorrelate.cpp:142-236.
  * src1, src2: CV_32FC1 rows x cols device images; window: same shape or
