@@ -47,6 +47,7 @@ _SIGNATURES = {
     "glsfft_phase_correlate": (_ip, [_vp, _vp, _vp, _vp, _ip, _ip, _ip, _dp, _dp, _dp, _vp]),
     "glsfft_phase_correlate_async": (_ip, [_vp, _vp, _vp, _vp, _ip, _ip, _ip, _vp, _vp]),
     "glsfft_phase_correlate_surface": (_ip, [_vp, _vp, _sz, _vp]),
+    "glsfft_phase_correlate_noalloc": (_ip, [_vp, _vp, _vp, _ip, _ip, _ip, _vp, _vp]),
 }
 
 _lib = None

@@ -222,6 +222,9 @@ const char *glsfft_status_string(int status) {
     case GLSFFT_ERROR_BUDGET: return "workspace would exceed the context's HBM budget";
     case GLSFFT_ERROR_TIMEOUT: return "bounded device-side wait expired";
     case GLSFFT_ERROR_SHAPE: return "inputs have different shapes";
+    case GLSFFT_ERROR_NOALLOC_LIMIT:
+        return "rows*cols exceeds the static scratch of glsfft_phase_correlate_noalloc "
+               "(GLSFFT_NOALLOC_MAX_PIXELS)";
     default: return "unknown status";
     }
 }

@@ -50,7 +50,8 @@ enum glsfft_status {
     GLSFFT_ERROR_OUT_OF_MEMORY = 6, /* device workspace allocation failed */
     GLSFFT_ERROR_BUDGET = 7,        /* workspace would exceed the context's HBM budget */
     GLSFFT_ERROR_TIMEOUT = 8,       /* a bounded device-side wait expired */
-    GLSFFT_ERROR_SHAPE = 9          /* inputs of different shapes */
+    GLSFFT_ERROR_SHAPE = 9,         /* inputs of different shapes */
+    GLSFFT_ERROR_NOALLOC_LIMIT = 10 /* rows*cols above GLSFFT_NOALLOC_MAX_PIXELS */
 };
 
 typedef struct glsfft_context_s *glsfft_context;
@@ -139,6 +140,41 @@ GLSFFT_API int glsfft_phase_correlate_async(glsfft_context ctx, const float *src
  */
 GLSFFT_API int glsfft_phase_correlate_surface(glsfft_context ctx, float *dst, size_t count,
                                               void *stream);
+
+/* Largest image (rows * cols) glsfft_phase_correlate_noalloc accepts. */
+#define GLSFFT_NOALLOC_MAX_PIXELS (512 * 512)
+
+/*
+ * phaseCorrelate that allocates no device memory at all.  No counterpart in
+ * the reference (glsCV always allocates textures); it exists for callers
+ * that may not call cudaMalloc: hosts whose device memory is owned by their
+ * own pool or budget (a framework's caching allocator, a plugin host that
+ * hands out buffers), where an allocation behind their back escapes that
+ * accounting or fails once the pool holds the rest of the device; and
+ * per-frame loops, where cudaMalloc/cudaFree synchronise the device and
+ * stall the pipeline.  It needs no context.
+ *
+ * Same computation and result layout as glsfft_phase_correlate_async:
+ * src1, src2 (and the optional window) are CV_32FC1 rows x cols device
+ * images; 5 doubles {dx, dy, response, peak index, peak value} are written
+ * to the device buffer d_result.  Its scratch (two spectra, the correlation
+ * surface and the argmax word: 20 * rows * cols bytes) is one statically
+ * sized device array of the library, so rows * cols must not exceed
+ * GLSFFT_NOALLOC_MAX_PIXELS (GLSFFT_ERROR_NOALLOC_LIMIT otherwise).  That
+ * array (5 MiB) and a 64 KiB twiddle table are held on every GPU that loads
+ * the library until the process exits.
+ *
+ * The first call on a device (the current device) sets up: it looks up the
+ * arrays' device addresses and uploads the twiddle table with a synchronous
+ * copy; make that first call before any stream capture.  Every call uses the
+ * same scratch array, which keeps the previous call's contents (the argmax
+ * word is cleared on each call), so calls whose work overlaps on the GPU --
+ * on different streams or from different host threads -- race: issue them
+ * on one stream.
+ */
+GLSFFT_API int glsfft_phase_correlate_noalloc(const float *src1, const float *src2,
+                                              const float *window, int rows, int cols, int box,
+                                              double *d_result, void *stream);
 
 #ifdef __cplusplus
 } /* extern "C" */
