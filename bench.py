@@ -241,26 +241,33 @@ def run_own(args) -> None:
     ptr_in = [d_in[i].data_ptr() for i in range(B)]
     ptr_out = [d_out[i].data_ptr() for i in range(B)]
 
-    launches_per_step = 4 * B
+    launches_per_step = 4
     ev = {}
+    base_in, base_out = d_in.data_ptr(), d_out.data_ptr()
 
     def step(record: bool):
-        # forward rows, forward cols, inverse rows, inverse cols (+SCALE):
-        # the two passes of gls::fft twice, timed per kernel
+        # batched path: forward rows, forward cols, inverse rows, inverse
+        # cols (+SCALE) -- the two passes of gls::fft twice, one launch per
+        # pass for the whole batch, timed per kernel
+        for kind, fn, src, flags in (("rows", ctx.fft_rows, base_in, 0),
+                                     ("cols", ctx.fft_cols, base_out, 0),
+                                     ("rows", ctx.fft_rows, base_out, INV),
+                                     ("cols", ctx.fft_cols, base_out, INV | SCALE)):
+            if record:
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                fn(src, base_out, ROWS, COLS, flags, s, count=B)
+                e1.record(stream)
+                ev.setdefault(kind, []).append((e0, e1))
+            else:
+                fn(src, base_out, ROWS, COLS, flags, s, count=B)
+
+    def plain_step():
+        # the same work through the plain per-image path (2 launches per transform)
         for i in range(B):
-            for kind, fn, src, flags in (("rows", ctx.fft_rows, ptr_in[i], 0),
-                                         ("cols", ctx.fft_cols, ptr_out[i], 0),
-                                         ("rows", ctx.fft_rows, ptr_out[i], INV),
-                                         ("cols", ctx.fft_cols, ptr_out[i], INV | SCALE)):
-                if record:
-                    e0 = torch.cuda.Event(enable_timing=True)
-                    e1 = torch.cuda.Event(enable_timing=True)
-                    e0.record(stream)
-                    fn(src, ptr_out[i], ROWS, COLS, flags, s)
-                    e1.record(stream)
-                    ev.setdefault(kind, []).append((e0, e1))
-                else:
-                    fn(src, ptr_out[i], ROWS, COLS, flags, s)
+            ctx.fft2d(ptr_in[i], ptr_out[i], ROWS, COLS, 0, s)
+            ctx.fft2d(ptr_out[i], ptr_out[i], ROWS, COLS, INV | SCALE, s)
 
     for _ in range(max(3, args.warmup)):
         step(False)
@@ -288,11 +295,26 @@ def run_own(args) -> None:
     avg = {k: sum(v) / len(v) for k, v in durs.items()}
     tot = {k: sum(v) for k, v in durs.items()}
     dom = max(tot, key=tot.get)
-    alg_bytes = 16.0 * ROWS * COLS  # one read + one write of 8-byte pixels per pass
+    # one read + one write of 8-byte pixels per pass, for all B images of a launch
+    alg_bytes = 16.0 * ROWS * COLS * B
     achieved = alg_bytes / (avg[dom] * 1e-3) / 1e9
     peak, peak_kind = measured_peaks()
-    kernel_name = {"rows": "fft_rows_kernel<1024>", "cols": "fft_cols_kernel<1024>"}[dom]
+    kernel_name = {"rows": f"fft_rows_kernel<1024>x{B}", "cols": f"fft_cols_kernel<1024>x{B}"}[dom]
     traffic = traffic_per_launch(kernel_name)
+
+    # the plain per-image path on the same batch (the >= 3x comparison)
+    plain_step()
+    torch.cuda.synchronize()
+    k_plain = max(1, min(args.steps, 3))
+    p0 = torch.cuda.Event(enable_timing=True)
+    p1 = torch.cuda.Event(enable_timing=True)
+    p0.record(stream)
+    for _ in range(k_plain):
+        plain_step()
+    p1.record(stream)
+    torch.cuda.synchronize()
+    plain_ms = max_over_ranks(p0.elapsed_time(p1) / k_plain)
+    plain_value = world * B * flops_per_image() / (plain_ms * 1e-3) / 1e9
 
     # accuracy of this run's first image vs FP64
     x0 = host[0].numpy()
@@ -313,9 +335,8 @@ def run_own(args) -> None:
 
         def e2e_step():
             d_in.copy_(host, non_blocking=True)
-            for i in range(B):
-                ctx.fft2d(ptr_in[i], ptr_out[i], ROWS, COLS, 0, s)
-                ctx.fft2d(ptr_out[i], ptr_out[i], ROWS, COLS, INV | SCALE, s)
+            ctx.fft2d_batched(base_in, base_out, B, ROWS, COLS, 0, s)
+            ctx.fft2d_batched(base_out, base_out, B, ROWS, COLS, INV | SCALE, s)
             host_out.copy_(d_out, non_blocking=True)
 
         e2e_step()
@@ -359,7 +380,11 @@ def run_own(args) -> None:
             "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": round(ms, 4),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic", "config": config(B, world),
-            "path": "plain per-image launches (rows kernel + columns kernel per transform)",
+            "path": "batched: one rows-pass and one columns-pass launch per transform for the "
+                    "whole batch (glsfft_fft_rows/cols, count=images)",
+            "plain_per_image": {"value": round(plain_value, 3), "unit": UNIT,
+                                "ms_per_step": round(plain_ms, 4),
+                                "speedup_of_value": round(value / plain_value, 3)},
             "rel_l2_vs_fp64": {"forward": rel_fwd, "round_trip": rel_rt},
             "roofline": {"bound": "hbm", "kernel": kernel_name, "achieved": round(achieved, 1),
                          "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),

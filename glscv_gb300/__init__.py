@@ -42,8 +42,9 @@ _SIGNATURES = {
     "glsfft_context_workspace": (_ip, [_vp, ctypes.POINTER(_sz)]),
     "glsfft_fft2d_c2c": (_ip, [_vp, _vp, _vp, _ip, _ip, _ip, _vp]),
     "glsfft_fft2d_r2c_promote": (_ip, [_vp, _vp, _vp, _ip, _ip, _ip, _vp]),
-    "glsfft_fft_rows": (_ip, [_vp, _vp, _vp, _ip, _ip, _ip, _vp]),
-    "glsfft_fft_cols": (_ip, [_vp, _vp, _vp, _ip, _ip, _ip, _vp]),
+    "glsfft_fft_rows": (_ip, [_vp, _vp, _vp, _ip, _ip, _ip, _ip, _vp]),
+    "glsfft_fft_cols": (_ip, [_vp, _vp, _vp, _ip, _ip, _ip, _ip, _vp]),
+    "glsfft_fft2d_batched": (_ip, [_vp, _vp, _vp, _ip, _ip, _ip, _ip, _vp]),
     "glsfft_phase_correlate": (_ip, [_vp, _vp, _vp, _vp, _ip, _ip, _ip, _dp, _dp, _dp, _vp]),
     "glsfft_phase_correlate_async": (_ip, [_vp, _vp, _vp, _vp, _ip, _ip, _ip, _vp, _vp]),
     "glsfft_phase_correlate_surface": (_ip, [_vp, _vp, _sz, _vp]),
@@ -116,13 +117,20 @@ class Context:
         fn = lib().glsfft_fft2d_r2c_promote if real_input else lib().glsfft_fft2d_c2c
         check(fn(self.handle, src, dst, rows, cols, flags, stream), "fft2d")
 
+    def fft2d_batched(self, src: int, dst: int, count: int, rows: int, cols: int,
+                      flags: int = 0, stream: int = 0) -> None:
+        check(lib().glsfft_fft2d_batched(self.handle, src, dst, count, rows, cols, flags, stream),
+              "fft2d_batched")
+
     def fft_rows(self, src: int, dst: int, rows: int, cols: int, flags: int = 0,
-                 stream: int = 0) -> None:
-        check(lib().glsfft_fft_rows(self.handle, src, dst, rows, cols, flags, stream), "fft_rows")
+                 stream: int = 0, count: int = 1) -> None:
+        check(lib().glsfft_fft_rows(self.handle, src, dst, count, rows, cols, flags, stream),
+              "fft_rows")
 
     def fft_cols(self, src: int, dst: int, rows: int, cols: int, flags: int = 0,
-                 stream: int = 0) -> None:
-        check(lib().glsfft_fft_cols(self.handle, src, dst, rows, cols, flags, stream), "fft_cols")
+                 stream: int = 0, count: int = 1) -> None:
+        check(lib().glsfft_fft_cols(self.handle, src, dst, count, rows, cols, flags, stream),
+              "fft_cols")
 
     # -- gls::phaseCorrelate -------------------------------------------------
     def phase_correlate(self, src1: int, src2: int, window: int | None, rows: int, cols: int,

@@ -101,13 +101,15 @@ int glsfft::ensure_workspace(glsfft_context ctx, size_t bytes) {
     return GLSFFT_SUCCESS;
 }
 
-// The two passes of gls::fft.  `real_in`: src is CV_32FC1 (promote).
+// The two passes of gls::fft over `count` back-to-back images (one launch
+// per pass for the whole batch).  `real_in`: src is CV_32FC1 (promote).
 int glsfft::fft2d_launch(glsfft_context ctx, const void *src, void *dst, int rows, int cols,
-                         int flags, bool real_in, cudaStream_t s) {
+                         int flags, bool real_in, cudaStream_t s, int count) {
     const bool inv = flags & GLSFFT_INVERSE, scale = flags & GLSFFT_SCALE,
                shift = flags & GLSFFT_SHIFT;
     const bool do_rows = cols > 1 || rows == 1 || real_in;
     const bool do_cols = rows > 1;
+    const size_t px = (size_t)rows * cols;
     if (do_rows) {
         PassArgs a{};
         a.in0 = src;
@@ -118,7 +120,9 @@ int glsfft::fft2d_launch(glsfft_context ctx, const void *src, void *dst, int row
         a.flags = (inv ? PF_CONJ_IN : 0u) | (inv && !do_cols ? PF_CONJ_OUT : 0u) |
                   (shift ? PF_SHIFT_COLS : 0u);
         a.tw = ctx->d_tw + cols;
-        cudaError_t e = launch_rows(cols, real_in ? LD_R1 : LD_C2, ST_C2, a, 1, s);
+        a.in_img_bytes = px * (real_in ? sizeof(float) : sizeof(float2));
+        a.out_img_bytes = px * sizeof(float2);
+        cudaError_t e = launch_rows(cols, real_in ? LD_R1 : LD_C2, ST_C2, a, count, s);
         if (e != cudaSuccess) return cuda_status(e);
     }
     if (do_cols) {
@@ -131,7 +135,8 @@ int glsfft::fft2d_launch(glsfft_context ctx, const void *src, void *dst, int row
         a.flags = (inv && !do_rows ? PF_CONJ_IN : 0u) | (inv ? PF_CONJ_OUT : 0u) |
                   (shift ? PF_SHIFT_ROWS : 0u);
         a.tw = ctx->d_tw + rows;
-        cudaError_t e = launch_cols(rows, LD_C2, ST_C2, a, 1, s);
+        a.in_img_bytes = a.out_img_bytes = px * sizeof(float2);
+        cudaError_t e = launch_cols(rows, LD_C2, ST_C2, a, count, s);
         if (e != cudaSuccess) return cuda_status(e);
     }
     return GLSFFT_SUCCESS;
@@ -304,10 +309,11 @@ int glsfft_fft2d_r2c_promote(glsfft_context ctx, const float *src, void *dst, in
     return fft2d_launch(ctx, src, dst, rows, cols, flags, true, (cudaStream_t)stream);
 }
 
-static int one_pass(glsfft_context ctx, const void *src, void *dst, int rows, int cols,
-                    int flags, bool along_rows, cudaStream_t s) {
+static int one_pass(glsfft_context ctx, const void *src, void *dst, int count, int rows,
+                    int cols, int flags, bool along_rows, cudaStream_t s) {
     int st = check_fft_args(src, dst, rows, cols, flags, false);
     if (st) return st;
+    if (count < 1 || count > kMaxBatch) return GLSFFT_ERROR_INVALID_VALUE;
     if (!ctx) return GLSFFT_ERROR_INVALID_VALUE;
     DeviceGuard g(ctx->device);
     if (!g.ok()) return GLSFFT_ERROR_CUDA;
@@ -322,19 +328,31 @@ static int one_pass(glsfft_context ctx, const void *src, void *dst, int rows, in
     a.flags = (inv ? PF_CONJ_IN | PF_CONJ_OUT : 0u) |
               ((flags & GLSFFT_SHIFT) ? (along_rows ? PF_SHIFT_COLS : PF_SHIFT_ROWS) : 0u);
     a.tw = ctx->d_tw + n;
-    cudaError_t e = along_rows ? launch_rows(n, LD_C2, ST_C2, a, 1, s)
-                               : launch_cols(n, LD_C2, ST_C2, a, 1, s);
+    a.in_img_bytes = a.out_img_bytes = (size_t)rows * cols * sizeof(float2);
+    cudaError_t e = along_rows ? launch_rows(n, LD_C2, ST_C2, a, count, s)
+                               : launch_cols(n, LD_C2, ST_C2, a, count, s);
     return cuda_status(e);
 }
 
-int glsfft_fft_rows(glsfft_context ctx, const void *src, void *dst, int rows, int cols,
-                    int flags, void *stream) {
-    return one_pass(ctx, src, dst, rows, cols, flags, true, (cudaStream_t)stream);
+int glsfft_fft_rows(glsfft_context ctx, const void *src, void *dst, int count, int rows,
+                    int cols, int flags, void *stream) {
+    return one_pass(ctx, src, dst, count, rows, cols, flags, true, (cudaStream_t)stream);
 }
 
-int glsfft_fft_cols(glsfft_context ctx, const void *src, void *dst, int rows, int cols,
-                    int flags, void *stream) {
-    return one_pass(ctx, src, dst, rows, cols, flags, false, (cudaStream_t)stream);
+int glsfft_fft_cols(glsfft_context ctx, const void *src, void *dst, int count, int rows,
+                    int cols, int flags, void *stream) {
+    return one_pass(ctx, src, dst, count, rows, cols, flags, false, (cudaStream_t)stream);
+}
+
+int glsfft_fft2d_batched(glsfft_context ctx, const void *src, void *dst, int count, int rows,
+                         int cols, int flags, void *stream) {
+    int st = check_fft_args(src, dst, rows, cols, flags, false);
+    if (st) return st;
+    if (count < 1 || count > kMaxBatch) return GLSFFT_ERROR_INVALID_VALUE;
+    if (!ctx) return GLSFFT_ERROR_INVALID_VALUE;
+    DeviceGuard g(ctx->device);
+    if (!g.ok()) return GLSFFT_ERROR_CUDA;
+    return fft2d_launch(ctx, src, dst, rows, cols, flags, false, (cudaStream_t)stream, count);
 }
 
 int glsfft_phase_correlate_async(glsfft_context ctx, const float *src1, const float *src2,

@@ -37,7 +37,9 @@ int check_fft_args(const void *src, const void *dst, int rows, int cols, int fla
 int check_poc_args(glsfft_context ctx, const float *src1, const float *src2,
                    const float *window, int rows, int cols, int box);
 int fft2d_launch(glsfft_context ctx, const void *src, void *dst, int rows, int cols, int flags,
-                 bool real_in, cudaStream_t s);
+                 bool real_in, cudaStream_t s, int count = 1);
+
+constexpr int kMaxBatch = 65535;  // grid y extent
 int poc_launch(const float2 *tw, const float *src1, const float *src2, const float *window,
                int rows, int cols, int box, float2 *f1, float2 *f2, float *surface,
                unsigned long long *key, double *d_result, cudaStream_t s);

@@ -38,6 +38,17 @@ struct ColSm {
     }
 };
 
+// Image z of a launch: in1/out1 when set (the two-image phaseCorrelate
+// launch), else image z of a contiguous batch starting at in0/out0.
+__device__ __forceinline__ const void *image_in(const PassArgs &a, unsigned z) {
+    if (z == 1 && a.in1) return a.in1;
+    return static_cast<const char *>(a.in0) + (size_t)z * a.in_img_bytes;
+}
+__device__ __forceinline__ void *image_out(const PassArgs &a, unsigned z) {
+    if (z == 1 && a.out1) return a.out1;
+    return static_cast<char *>(a.out0) + (size_t)z * a.out_img_bytes;
+}
+
 // ------------------------------------------------------------ load / store
 template <int LD>
 __device__ __forceinline__ float2 load_elem(const void *img, const float *win, size_t idx) {
@@ -52,7 +63,7 @@ __device__ __forceinline__ float2 load_elem(const void *img, const float *win, s
 }
 
 // ------------------------------------------------------------- row pass
-// Block: LINES rows x T threads.  blockIdx.y selects image 0 or 1.
+// Block: LINES rows x T threads.  blockIdx.y selects the image.
 template <int N, int E, int LINES, int LD, int ST>
 __global__ void __launch_bounds__(LINES *LineFft<N, E>::T)
     fft_rows_kernel(PassArgs a) {
@@ -65,8 +76,8 @@ __global__ void __launch_bounds__(LINES *LineFft<N, E>::T)
     const int l = threadIdx.x / T, t = threadIdx.x % T;
     const int row = blockIdx.x * LINES + l;
     const bool active = row < a.rows;
-    const void *in = blockIdx.y ? a.in1 : a.in0;
-    void *out = blockIdx.y ? a.out1 : a.out0;
+    const void *in = image_in(a, blockIdx.y);
+    void *out = image_out(a, blockIdx.y);
     const bool conj_in = a.flags & PF_CONJ_IN;
 
     float2 x[E];
@@ -115,8 +126,8 @@ __global__ void __launch_bounds__(W *LineFft<N, E>::T)
     const int col = blockIdx.x * W + c;
     const int cols = a.cols;
     const bool active = col < cols;
-    const void *in = blockIdx.y ? a.in1 : a.in0;
-    void *out = blockIdx.y ? a.out1 : a.out0;
+    const void *in = image_in(a, blockIdx.y);
+    void *out = image_out(a, blockIdx.y);
     const bool conj_in = a.flags & PF_CONJ_IN;
 
     float2 x[E];

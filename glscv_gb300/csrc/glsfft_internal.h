@@ -33,10 +33,12 @@ struct PassArgs {
     unsigned flags;
     unsigned long long *key;
     const float2 *tw;  // twiddle table of this pass's length
+    size_t in_img_bytes;   // batch: byte stride between images (0 = single / in1 mode)
+    size_t out_img_bytes;
 };
 
 // Launchers (fft_rows.cu, fft_cols.cu, poc.cu).  They return cudaSuccess or
-// the launch error; `images` is 1 or 2 (blockIdx.y selects in0/in1).
+// the launch error; `images` is the grid's y extent (blockIdx.y = image).
 cudaError_t launch_rows(int n, int ld, int st, const PassArgs &a, int images, cudaStream_t s);
 cudaError_t launch_cols(int n, int ld, int st, const PassArgs &a, int images, cudaStream_t s);
 cudaError_t launch_poc_cols(int n, const PassArgs &a, cudaStream_t s);

@@ -96,17 +96,28 @@ GLSFFT_API int glsfft_fft2d_r2c_promote(glsfft_context ctx, const float *src, vo
                                         int rows, int cols, int flags, void *stream);
 
 /*
- * One pass of gls::fft on its own: a 1-D FFT of every row (length cols) --
- * the rows pass, glsFft.cpp:561-605 -- or of every column (length rows) --
- * the columns pass, glsFft.cpp:607-652.  INVERSE conjugates input and output
- * of each line, SCALE multiplies by 1/length, SHIFT swaps the halves of each
- * line.  fft2d(flags) equals fft_rows then fft_cols with the same flags.
- * One kernel launch each; src == dst allowed.
+ * Batched gls::fft: `count` (1..65535) CV_32FC2 rows x cols images stored back
+ * to back (image i at byte offset i*rows*cols*8 of src and dst), each
+ * transformed as glsfft_fft2d_c2c does, with one launch per pass for the
+ * whole batch.  No reference counterpart (glsCV transforms one texture per
+ * call); src == dst allowed.
  */
-GLSFFT_API int glsfft_fft_rows(glsfft_context ctx, const void *src, void *dst, int rows,
-                               int cols, int flags, void *stream);
-GLSFFT_API int glsfft_fft_cols(glsfft_context ctx, const void *src, void *dst, int rows,
-                               int cols, int flags, void *stream);
+GLSFFT_API int glsfft_fft2d_batched(glsfft_context ctx, const void *src, void *dst, int count,
+                                    int rows, int cols, int flags, void *stream);
+
+/*
+ * One pass of gls::fft on its own, over `count` back-to-back images: a 1-D
+ * FFT of every row (length cols) -- the rows pass, glsFft.cpp:561-605 -- or
+ * of every column (length rows) -- the columns pass, glsFft.cpp:607-652.
+ * INVERSE conjugates input and output of each line, SCALE multiplies by
+ * 1/length, SHIFT swaps the halves of each line.  fft2d(flags) equals
+ * fft_rows then fft_cols with the same flags.  One kernel launch each;
+ * src == dst allowed.
+ */
+GLSFFT_API int glsfft_fft_rows(glsfft_context ctx, const void *src, void *dst, int count,
+                               int rows, int cols, int flags, void *stream);
+GLSFFT_API int glsfft_fft_cols(glsfft_context ctx, const void *src, void *dst, int count,
+                               int rows, int cols, int flags, void *stream);
 
 /*
  * gls::phaseCorrelate(src1, src2, window, &response),
