@@ -49,6 +49,17 @@ _SIGNATURES = {
     "glsfft_phase_correlate_async": (_ip, [_vp, _vp, _vp, _vp, _ip, _ip, _ip, _vp, _vp]),
     "glsfft_phase_correlate_surface": (_ip, [_vp, _vp, _sz, _vp]),
     "glsfft_phase_correlate_noalloc": (_ip, [_vp, _vp, _vp, _ip, _ip, _ip, _vp, _vp]),
+    "glsfft_batch_create": (_ip, [_vp, _ip, ctypes.POINTER(_vp), ctypes.POINTER(_vp),
+                                  ctypes.POINTER(_ip), ctypes.POINTER(_ip), _ip,
+                                  ctypes.POINTER(_ip), ctypes.POINTER(_vp)]),
+    "glsfft_batch_execute": (_ip, [_vp, _vp]),
+    "glsfft_batch_set_variant": (_ip, [_vp, _ip]),
+    "glsfft_batch_set_schedule": (_ip, [_vp, _ip, _ip, _ip]),
+    "glsfft_batch_status": (_ip, [_vp, _vp]),
+    "glsfft_batch_info": (_ip, [_vp, ctypes.POINTER(_ip), ctypes.POINTER(_ip),
+                                ctypes.POINTER(_ip)]),
+    "glsfft_batch_inject_stall": (_ip, [_vp, ctypes.c_longlong]),
+    "glsfft_batch_destroy": (_ip, [_vp]),
 }
 
 _lib = None
@@ -157,3 +168,60 @@ class Context:
 
     def set_budget(self, nbytes: int) -> None:
         check(lib().glsfft_context_set_budget(self.handle, nbytes), "set_budget")
+
+
+class Batch:
+    """A batch plan (glsfft_batch): uneven-size images through 1-2 transforms,
+    one persistent launch, captured into a CUDA graph."""
+
+    def __init__(self, ctx: Context, srcs, dsts, shapes, flags=(0,)):
+        n = len(srcs)
+        self.handle = _vp()
+        arr_v = _vp * n
+        arr_i = _ip * n
+        rows = arr_i(*[int(r) for r, _ in shapes])
+        cols = arr_i(*[int(c) for _, c in shapes])
+        fl = (_ip * len(flags))(*[int(f) for f in flags])
+        check(lib().glsfft_batch_create(ctx.handle, n, arr_v(*srcs), arr_v(*dsts), rows, cols,
+                                        len(flags), fl, ctypes.byref(self.handle)),
+              "glsfft_batch_create")
+
+    def execute(self, stream: int = 0) -> None:
+        check(lib().glsfft_batch_execute(self.handle, stream), "batch_execute")
+
+    def set_variant(self, variant: int) -> None:
+        check(lib().glsfft_batch_set_variant(self.handle, int(variant)), "batch_set_variant")
+
+    def set_schedule(self, claim_chunk: int = 1, claim_ahead: bool = False,
+                     lag_items: int = 0) -> None:
+        check(lib().glsfft_batch_set_schedule(self.handle, int(claim_chunk), int(claim_ahead),
+                                              int(lag_items)), "batch_set_schedule")
+
+    def status(self, stream: int = 0) -> int:
+        return int(lib().glsfft_batch_status(self.handle, stream))
+
+    def info(self):
+        a, b, c = _ip(), _ip(), _ip()
+        check(lib().glsfft_batch_info(self.handle, ctypes.byref(a), ctypes.byref(b),
+                                      ctypes.byref(c)), "batch_info")
+        return {"persistent_images": a.value, "items": b.value, "grid": c.value}
+
+    def inject_stall(self, wait_limit_ns: int) -> None:
+        check(lib().glsfft_batch_inject_stall(self.handle, int(wait_limit_ns)), "inject_stall")
+
+    def close(self) -> None:
+        if self.handle:
+            lib().glsfft_batch_destroy(self.handle)
+            self.handle = _vp()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,395 @@
+// batch.cpp -- batch plans: uneven-size images, each run through one or two
+// gls::fft transforms, executed as one CUDA graph.  Images the persistent
+// kernels cover (16 <= rows <= 1024, 16 <= cols <= 4096, 16-byte aligned
+// buffers) go through one persistent launch fed by a work list; any other
+// image gets its own pass launches inside the same graph.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+#include <cstdint>
+#include <cstring>
+#include <deque>
+#include <mutex>
+#include <new>
+#include <vector>
+
+#include "batch_internal.h"
+#include "capi_internal.h"
+#include "fft_config.h"
+#include "glsfft_internal.h"
+
+using namespace glsfft;
+
+struct glsfft_batch_s {
+    glsfft_context ctx = nullptr;
+    int device = 0;
+    int n_images = 0;      // images in the persistent launch
+    int n_items = 0;
+    int grid = 0;
+    int variant = BATCH_TMA_WS1;
+    void *d_mem = nullptr;  // tensor maps | images | passes | items | head, done, error
+    BatchArgs args{};
+    std::vector<BatchImage> images;
+    std::vector<BatchPass> passes;
+    struct Other {
+        const void *src;
+        void *dst;
+        int rows, cols;
+    };
+    std::vector<Other> others;  // images outside the persistent kernels' shapes
+    std::vector<int> flags;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    long long wait_limit_ns = 2000000000LL;
+    size_t o_items = 0;
+};
+
+namespace {
+
+int row_tiles_of(int rows, int cols) {
+    const int lines = kBatchTileElems / cols;
+    return (rows + lines - 1) / lines;
+}
+int col_tiles_of(int rows, int cols) {
+    const int w = kBatchTileElems / rows;
+    return (cols + w - 1) / w;
+}
+
+// Item order: pass 0 of the images in order; pass p+1 of an image enters the
+// list once `lag` items have been listed after its pass p (the work resident
+// blocks are busy with in the meantime), so its inputs are fresh in L2 and
+// rarely still being written.
+std::vector<BatchItem> order_items(const std::vector<BatchImage> &ims,
+                                   const std::vector<BatchPass> &passes, int lag) {
+    struct Pending {
+        size_t ready_at;
+        int image, pass, need;
+    };
+    std::vector<BatchItem> out;
+    std::deque<Pending> pend;  // ready_at is non-decreasing in push order
+    auto tiles = [&](int i, int p) {
+        return passes[p].along_rows ? ims[i].row_tiles : ims[i].col_tiles;
+    };
+    auto emit = [&](int i, int p, int need) {
+        const int n = tiles(i, p);
+        for (int t = 0; t < n; t++) out.push_back(BatchItem{i, p, t, need});
+        if (p + 1 < (int)passes.size())
+            pend.push_back(Pending{out.size() + (size_t)lag, i, p + 1, n});
+    };
+    for (int i = 0; i < (int)ims.size(); i++) {
+        while (!pend.empty() && pend.front().ready_at <= out.size()) {
+            Pending q = pend.front();
+            pend.pop_front();
+            emit(q.image, q.pass, q.need);
+        }
+        emit(i, 0, 0);
+    }
+    while (!pend.empty()) {
+        Pending q = pend.front();
+        pend.pop_front();
+        emit(q.image, q.pass, q.need);
+    }
+    return out;
+}
+
+int grid_for(int device, int variant) {
+    if (variant == BATCH_PLAIN) return batch_persistent_grid(device);
+    return batch_ws_grid(device, variant == BATCH_TMA_WS2 ? 2 : 1);
+}
+
+int record(glsfft_batch plan, cudaStream_t s) {
+    if (plan->n_images > 0) {
+        const size_t state = sizeof(unsigned) * (1 + (size_t)plan->n_images * kBatchMaxPasses) +
+                             sizeof(int);
+        cudaError_t e = cudaMemsetAsync(plan->args.head, 0, state, s);
+        if (e != cudaSuccess) return cuda_status(e);
+        if (plan->variant == BATCH_PLAIN)
+            e = launch_batch_persistent(plan->args, plan->grid, s);
+        else
+            e = launch_batch_ws(plan->args, plan->grid, plan->variant == BATCH_TMA_WS2 ? 2 : 1, s);
+        if (e != cudaSuccess) return cuda_status(e);
+    }
+    for (const auto &o : plan->others) {
+        const void *src = o.src;
+        for (int f : plan->flags) {
+            int st = fft2d_launch(plan->ctx, src, o.dst, o.rows, o.cols, f, false, s, 1);
+            if (st) return st;
+            src = o.dst;
+        }
+    }
+    return GLSFFT_SUCCESS;
+}
+
+// (Re)capture the plan into a graph and instantiate it.
+int capture(glsfft_batch plan) {
+    if (plan->exec) cudaGraphExecDestroy(plan->exec);
+    if (plan->graph) cudaGraphDestroy(plan->graph);
+    plan->exec = nullptr;
+    plan->graph = nullptr;
+    cudaStream_t cs = nullptr;
+    cudaError_t e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return cuda_status(e);
+    int st = GLSFFT_SUCCESS;
+    e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeRelaxed);
+    if (e != cudaSuccess) {
+        st = cuda_status(e);
+    } else {
+        int rst = record(plan, cs);
+        e = cudaStreamEndCapture(cs, &plan->graph);
+        if (rst) st = rst;
+        else if (e != cudaSuccess) st = cuda_status(e);
+        if (!st) {
+            e = cudaGraphInstantiate(&plan->exec, plan->graph, 0);
+            if (e != cudaSuccess) st = cuda_status(e);
+        }
+    }
+    cudaStreamDestroy(cs);
+    cudaGetLastError();
+    return st;
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 tmap_encoder() {
+    static std::once_flag once;
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    std::call_once(once, [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000,
+                                             cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    });
+    return fn;
+}
+
+}  // namespace
+
+int glsfft::make_column_tmap(void *tmap128, const void *img, int rows, int cols) {
+    auto enc = tmap_encoder();
+    if (!enc) return GLSFFT_ERROR_CUDA;
+    const int w = kBatchTileElems / rows;     // columns per tile
+    const int br = rows < 256 ? rows : 256;   // box height (TMA box dims <= 256)
+    cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+    cuuint64_t strides[1] = {(cuuint64_t)cols * sizeof(float2)};
+    cuuint32_t box[2] = {(cuuint32_t)w, (cuuint32_t)br};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = enc(reinterpret_cast<CUtensorMap *>(tmap128), CU_TENSOR_MAP_DATA_TYPE_UINT64, 2,
+                     const_cast<void *>(img), dims, strides, box, estr,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                     CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS ? GLSFFT_SUCCESS : GLSFFT_ERROR_CUDA;
+}
+
+extern "C" {
+
+int glsfft_batch_create(glsfft_context ctx, int count, const void *const *srcs,
+                        void *const *dsts, const int *rows, const int *cols, int n_transforms,
+                        const int *flags, glsfft_batch *out) {
+    if (!out) return GLSFFT_ERROR_INVALID_VALUE;
+    *out = nullptr;
+    if (!srcs || !dsts || !rows || !cols || !flags || count < 1) return GLSFFT_ERROR_INVALID_VALUE;
+    if (n_transforms < 1 || n_transforms > kBatchMaxPasses / 2) return GLSFFT_ERROR_INVALID_VALUE;
+    for (int k = 0; k < n_transforms; k++) {
+        if (flags[k] & ~(GLSFFT_INVERSE | GLSFFT_SCALE | GLSFFT_SHIFT))
+            return GLSFFT_ERROR_INVALID_VALUE;
+    }
+    for (int i = 0; i < count; i++) {
+        int st = check_fft_args(srcs[i], dsts[i], rows[i], cols[i], 0, false);
+        if (st) return st;
+    }
+    if (!ctx) return GLSFFT_ERROR_INVALID_VALUE;
+    DeviceGuard g(ctx->device);
+    if (!g.ok()) return GLSFFT_ERROR_CUDA;
+
+    auto *plan = new (std::nothrow) glsfft_batch_s();
+    if (!plan) return GLSFFT_ERROR_OUT_OF_MEMORY;
+    plan->ctx = ctx;
+    plan->device = ctx->device;
+    plan->flags.assign(flags, flags + n_transforms);
+
+    // the pass chain: rows then columns per transform, gls::fft's flags split
+    // per pass exactly as glsfft_fft2d_c2c does for a 2-D image
+    for (int k = 0; k < n_transforms; k++) {
+        const bool inv = flags[k] & GLSFFT_INVERSE, sc = flags[k] & GLSFFT_SCALE,
+                   sh = flags[k] & GLSFFT_SHIFT;
+        plan->passes.push_back(BatchPass{1, (inv ? PF_CONJ_IN : 0u) | (sh ? PF_SHIFT_COLS : 0u), sc, 0});
+        plan->passes.push_back(BatchPass{0, (inv ? PF_CONJ_OUT : 0u) | (sh ? PF_SHIFT_ROWS : 0u), sc, 0});
+    }
+
+    for (int i = 0; i < count; i++) {
+        const bool aligned16 = ((reinterpret_cast<uintptr_t>(srcs[i]) |
+                                 reinterpret_cast<uintptr_t>(dsts[i])) & 15) == 0;
+        if (batch_supported(rows[i], cols[i]) && aligned16) {
+            BatchImage im{};
+            im.src = static_cast<const float2 *>(srcs[i]);
+            im.dst = static_cast<float2 *>(dsts[i]);
+            im.rows = rows[i];
+            im.cols = cols[i];
+            im.row_tiles = row_tiles_of(rows[i], cols[i]);
+            im.col_tiles = col_tiles_of(rows[i], cols[i]);
+            plan->images.push_back(im);
+        } else {
+            plan->others.push_back({srcs[i], dsts[i], rows[i], cols[i]});
+        }
+    }
+    plan->n_images = (int)plan->images.size();
+    int st = GLSFFT_SUCCESS;
+    if (plan->n_images > 0) {
+        plan->grid = grid_for(ctx->device, plan->variant);
+        if (plan->grid <= 0) st = GLSFFT_ERROR_CUDA;
+        std::vector<BatchItem> items;
+        if (!st) items = order_items(plan->images, plan->passes, plan->grid);
+        plan->n_items = (int)items.size();
+        const size_t ni = plan->images.size();
+        const size_t b_tm = 128 * ni;
+        const size_t b_im = sizeof(BatchImage) * ni;
+        const size_t b_ps = sizeof(BatchPass) * plan->passes.size();
+        const size_t b_it = sizeof(BatchItem) * items.size();
+        const size_t b_state = sizeof(unsigned) * (1 + ni * kBatchMaxPasses) + sizeof(int);
+        auto up = [](size_t x) { return (x + 255) / 256 * 256; };
+        const size_t o_im = up(b_tm), o_ps = o_im + up(b_im), o_it = o_ps + up(b_ps),
+                     o_st = o_it + up(b_it), total = o_st + b_state;
+        plan->o_items = o_it;
+        if (!st && ctx->budget && total > ctx->budget) st = GLSFFT_ERROR_BUDGET;
+        if (!st && cudaMalloc(&plan->d_mem, total) != cudaSuccess) {
+            cudaGetLastError();
+            st = GLSFFT_ERROR_OUT_OF_MEMORY;
+        }
+        if (!st) {
+            std::vector<unsigned char> host(o_st, 0);
+            for (size_t i = 0; i < ni && !st; i++)
+                st = make_column_tmap(host.data() + 128 * i, plan->images[i].dst,
+                                      plan->images[i].rows, plan->images[i].cols);
+            std::memcpy(host.data() + o_im, plan->images.data(), b_im);
+            std::memcpy(host.data() + o_ps, plan->passes.data(), b_ps);
+            std::memcpy(host.data() + o_it, items.data(), b_it);
+            char *base = static_cast<char *>(plan->d_mem);
+            if (!st) {
+                cudaError_t e = cudaMemcpy(base, host.data(), o_st, cudaMemcpyHostToDevice);
+                if (e != cudaSuccess) st = cuda_status(e);
+            }
+            BatchArgs &a = plan->args;
+            a.tmaps = base;
+            a.images = reinterpret_cast<const BatchImage *>(base + o_im);
+            a.passes = reinterpret_cast<const BatchPass *>(base + o_ps);
+            a.items = reinterpret_cast<const BatchItem *>(base + o_it);
+            a.n_items = plan->n_items;
+            a.n_passes = (int)plan->passes.size();
+            a.head = reinterpret_cast<unsigned *>(base + o_st);
+            a.done = a.head + 1;
+            a.error = reinterpret_cast<int *>(a.done + ni * kBatchMaxPasses);
+            a.tw = ctx->d_tw;
+            a.wait_limit_ns = plan->wait_limit_ns;
+            a.claim_chunk = 1;
+            a.claim_ahead = 0;
+        }
+    }
+    if (!st) st = capture(plan);
+    if (st) {
+        if (plan->exec) cudaGraphExecDestroy(plan->exec);
+        if (plan->graph) cudaGraphDestroy(plan->graph);
+        if (plan->d_mem) cudaFree(plan->d_mem);
+        delete plan;
+        return st;
+    }
+    *out = plan;
+    return GLSFFT_SUCCESS;
+}
+
+int glsfft_batch_set_variant(glsfft_batch plan, int variant) {
+    if (!plan || variant < BATCH_PLAIN || variant > BATCH_TMA_WS2) return GLSFFT_ERROR_INVALID_VALUE;
+    DeviceGuard g(plan->device);
+    if (!g.ok()) return GLSFFT_ERROR_CUDA;
+    if (plan->n_images > 0) {
+        const int grid = grid_for(plan->device, variant);
+        if (grid <= 0) return GLSFFT_ERROR_CUDA;
+        if (grid != plan->grid) {
+            // the item order's lag follows the resident grid
+            std::vector<BatchItem> items = order_items(plan->images, plan->passes, grid);
+            cudaError_t e = cudaMemcpy(static_cast<char *>(plan->d_mem) + plan->o_items,
+                                       items.data(), sizeof(BatchItem) * items.size(),
+                                       cudaMemcpyHostToDevice);
+            if (e != cudaSuccess) return cuda_status(e);
+            plan->grid = grid;
+        }
+    }
+    plan->variant = variant;
+    return capture(plan);
+}
+
+int glsfft_batch_set_schedule(glsfft_batch plan, int claim_chunk, int claim_ahead, int lag_blocks) {
+    if (!plan || claim_chunk < 1 || claim_chunk > 4 || lag_blocks < 0)
+        return GLSFFT_ERROR_INVALID_VALUE;
+    DeviceGuard g(plan->device);
+    if (!g.ok()) return GLSFFT_ERROR_CUDA;
+    plan->args.claim_chunk = claim_chunk;
+    plan->args.claim_ahead = claim_ahead ? 1 : 0;
+    if (plan->n_images > 0 && lag_blocks > 0) {
+        std::vector<BatchItem> items = order_items(plan->images, plan->passes, lag_blocks);
+        cudaError_t e = cudaMemcpy(static_cast<char *>(plan->d_mem) + plan->o_items, items.data(),
+                                   sizeof(BatchItem) * items.size(), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) return cuda_status(e);
+    }
+    return capture(plan);
+}
+
+int glsfft_batch_execute(glsfft_batch plan, void *stream) {
+    if (!plan) return GLSFFT_ERROR_INVALID_VALUE;
+    DeviceGuard g(plan->device);
+    if (!g.ok()) return GLSFFT_ERROR_CUDA;
+    return cuda_status(cudaGraphLaunch(plan->exec, (cudaStream_t)stream));
+}
+
+int glsfft_batch_status(glsfft_batch plan, void *stream) {
+    if (!plan) return GLSFFT_ERROR_INVALID_VALUE;
+    if (plan->n_images == 0) return GLSFFT_SUCCESS;
+    DeviceGuard g(plan->device);
+    if (!g.ok()) return GLSFFT_ERROR_CUDA;
+    int err = 0;
+    cudaError_t e = cudaMemcpyAsync(&err, plan->args.error, sizeof(int), cudaMemcpyDeviceToHost,
+                                    (cudaStream_t)stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize((cudaStream_t)stream);
+    if (e != cudaSuccess) return cuda_status(e);
+    return err;
+}
+
+int glsfft_batch_info(glsfft_batch plan, int *persistent_images, int *items, int *grid) {
+    if (!plan) return GLSFFT_ERROR_INVALID_VALUE;
+    if (persistent_images) *persistent_images = plan->n_images;
+    if (items) *items = plan->n_items;
+    if (grid) *grid = plan->grid;
+    return GLSFFT_SUCCESS;
+}
+
+int glsfft_batch_inject_stall(glsfft_batch plan, long long wait_limit_ns) {
+    // host-side fault injection: the last item of the list waits for one more
+    // tile than its previous pass has, so its bounded wait must expire
+    if (!plan || plan->n_images == 0 || plan->n_items < 1 || wait_limit_ns <= 0)
+        return GLSFFT_ERROR_INVALID_VALUE;
+    DeviceGuard g(plan->device);
+    if (!g.ok()) return GLSFFT_ERROR_CUDA;
+    BatchItem last{};
+    const BatchItem *d_last = plan->args.items + plan->n_items - 1;
+    cudaError_t e = cudaMemcpy(&last, d_last, sizeof(last), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_status(e);
+    if (last.pass == 0) return GLSFFT_ERROR_INVALID_VALUE;
+    last.need += 1;
+    e = cudaMemcpy(const_cast<BatchItem *>(d_last), &last, sizeof(last), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return cuda_status(e);
+    // the deadline is a kernel argument baked into the graph: re-capture
+    plan->wait_limit_ns = wait_limit_ns;
+    plan->args.wait_limit_ns = wait_limit_ns;
+    return capture(plan);
+}
+
+int glsfft_batch_destroy(glsfft_batch plan) {
+    if (!plan) return GLSFFT_ERROR_INVALID_VALUE;
+    DeviceGuard g(plan->device);
+    if (plan->exec) cudaGraphExecDestroy(plan->exec);
+    if (plan->graph) cudaGraphDestroy(plan->graph);
+    if (plan->d_mem) cudaFree(plan->d_mem);
+    delete plan;
+    return GLSFFT_SUCCESS;
+}
+
+}  // extern "C"

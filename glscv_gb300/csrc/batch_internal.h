@@ -1,0 +1,74 @@
+// batch_internal.h -- data shared by the persistent batched FFT kernel and its
+// host-side plan (batch.cu).  Not a public header.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace glsfft {
+
+constexpr int kBatchThreads = 256;      // threads of a persistent block
+constexpr int kBatchTileElems = 4096;   // complex values per tile (16 per thread)
+constexpr int kBatchMaxPasses = 4;      // passes per image (2 transforms)
+
+// One image of a batch plan.  Pass 0 reads src; every later pass reads and
+// writes dst (in place), so src may equal dst.
+struct BatchImage {
+    const float2 *src;
+    float2 *dst;
+    int rows, cols;
+    int row_tiles, col_tiles;  // tiles of a rows pass / a columns pass
+    int pad0, pad1;
+};
+
+// One pass of the chain every image runs through.
+struct BatchPass {
+    int along_rows;  // 1: 1-D FFT of every row, 0: of every column
+    unsigned flags;  // PF_CONJ_IN / PF_CONJ_OUT / PF_SHIFT_ROWS / PF_SHIFT_COLS
+    int scale;       // 1: multiply by 1/length
+    int pad;
+};
+
+// Work item: image, pass, tile, and how many tiles of the previous pass of
+// the same image must be complete first (0 for pass 0).
+struct BatchItem {
+    int image;
+    int pass;
+    int tile;
+    int need;
+};
+
+struct BatchArgs {
+    const BatchImage *images;
+    const BatchPass *passes;
+    const BatchItem *items;
+    int n_items;
+    int n_passes;
+    unsigned *head;        // next item index (zeroed before each launch)
+    unsigned *done;        // [image * kBatchMaxPasses + pass] completed tiles (zeroed)
+    int *error;            // set to a non-zero code when a bounded wait expires
+    const float2 *tw;      // twiddle tables (entries [n, 2n) for length n)
+    long long wait_limit_ns;  // bound on one dependency wait
+    const void *tmaps;     // warp-specialised kernel: one 128-B CUtensorMap per image (dst)
+    int claim_chunk;       // warp-specialised kernel: items claimed per queue atomic (1..4)
+    int claim_ahead;       // 1: claim the next chunk before working on the current one
+};
+
+// Persistent kernel variants: plain (every thread loads its operands) and
+// warp-specialised (a producer warp stages tiles with TMA into a 3-stage
+// shared-memory ring; eight compute warps run the FFT and store).
+// The warp-specialised kernel comes compiled for 1 and for 2 blocks per SM
+// (at 2, nine warps per block cap registers at 96 and the FFT spills a little).
+enum { BATCH_PLAIN = 0, BATCH_TMA_WS1 = 1, BATCH_TMA_WS2 = 2 };
+
+cudaError_t launch_batch_persistent(const BatchArgs &a, int grid, cudaStream_t s);
+int batch_persistent_grid(int device);  // blocks that fit on the device at once
+bool batch_supported(int rows, int cols);
+
+cudaError_t launch_batch_ws(const BatchArgs &a, int grid, int blocks_per_sm, cudaStream_t s);
+int batch_ws_grid(int device, int blocks_per_sm);
+
+// Build the 2-D tensor map (8-byte elements, box W x min(rows, 256)) that the
+// warp-specialised kernel uses to stage column tiles of `img` (rows x cols).
+int make_column_tmap(void *tmap128, const void *img, int rows, int cols);
+
+}  // namespace glsfft

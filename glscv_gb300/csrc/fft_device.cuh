@@ -134,9 +134,20 @@ template <> struct Dft<16> {
 };
 
 // ------------------------------------------------------- the line engine
+// Barrier policies for the exchanges: the whole block, or only the 256
+// compute threads of a warp-specialised block (named barrier 1).
+struct SyncBlock {
+    __device__ __forceinline__ void operator()() const { __syncthreads(); }
+};
+struct SyncCompute256 {
+    __device__ __forceinline__ void operator()() const {
+        asm volatile("bar.sync 1, 256;" ::: "memory");
+    }
+};
+
 // Sm: shared-memory accessor, sm(pos) -> float2& for this thread's line.
 // tw: twiddle table for length N, tw[k] = e^{-2 pi i k/N}, k < N.
-template <int N, int E>
+template <int N, int E, class Sync = SyncBlock>
 struct LineFft {
     static_assert((N & (N - 1)) == 0 && N >= 1 && N <= 8192, "N must be a power of two");
     static_assert(N == 1 || (N % E) == 0, "E must divide N");
@@ -153,6 +164,7 @@ struct LineFft {
     __device__ __forceinline__ static void pass(float2 (&x)[E], int t, Sm sm,
                                                 const float2 *__restrict__ tw) {
         if constexpr (p < P) {
+            [[maybe_unused]] const Sync sync{};
             constexpr int R = pass_radix(N, p);
             constexpr int Ns = pass_span(N, p);
             constexpr int S = E / R;
@@ -181,10 +193,10 @@ struct LineFft {
                 }
             }
             if constexpr (!last) {
-                __syncthreads();
+                sync();
 #pragma unroll
                 for (int m = 0; m < E; m++) x[m] = sm(t + m * T);
-                __syncthreads();
+                sync();
                 pass<p + 1>(x, t, sm, tw);
             }
         }

@@ -119,6 +119,69 @@ GLSFFT_API int glsfft_fft_rows(glsfft_context ctx, const void *src, void *dst, i
 GLSFFT_API int glsfft_fft_cols(glsfft_context ctx, const void *src, void *dst, int count,
                                int rows, int cols, int flags, void *stream);
 
+typedef struct glsfft_batch_s *glsfft_batch;
+
+/*
+ * Batch plan: `count` CV_32FC2 device images of individual sizes (srcs[i] ->
+ * dsts[i], rows[i] x cols[i]; src may equal dst), each run through
+ * n_transforms (1 or 2) successive gls::fft transforms with flags[k] (e.g.
+ * {0, GLSFFT_INVERSE | GLSFFT_SCALE}: forward, then back).  Images with
+ * 16 <= rows <= 1024 and 16 <= cols <= 4096 are processed by one persistent
+ * launch that pulls (image, pass, tile) items from a work list, each pass of
+ * an image waiting (bounded) for that image's previous pass; other shapes get
+ * their own pass launches.  Everything is captured once into a CUDA graph.
+ * No reference counterpart (glsCV transforms one texture per call).  The
+ * plan keeps the pointers: the buffers must outlive it.
+ */
+GLSFFT_API int glsfft_batch_create(glsfft_context ctx, int count, const void *const *srcs,
+                                   void *const *dsts, const int *rows, const int *cols,
+                                   int n_transforms, const int *flags, glsfft_batch *plan);
+
+/* Launch the plan's graph on `stream` (asynchronous). */
+GLSFFT_API int glsfft_batch_execute(glsfft_batch plan, void *stream);
+
+/*
+ * Persistent-kernel schedule of a plan (re-captures its graph):
+ * 0 = every thread loads its own operands (2 blocks/SM);
+ * 1 = warp-specialised: a producer warp stages tiles with TMA into a 3-stage
+ *     shared-memory ring for 8 compute warps (1 block/SM, the default);
+ * 2 = the same at 2 blocks/SM (registers capped, some spilling).
+ */
+#define GLSFFT_BATCH_PLAIN 0
+#define GLSFFT_BATCH_TMA_WS1 1
+#define GLSFFT_BATCH_TMA_WS2 2
+GLSFFT_API int glsfft_batch_set_variant(glsfft_batch plan, int variant);
+
+/*
+ * Work-queue schedule of a plan (re-captures its graph): items claimed per
+ * queue atomic by a warp-specialised block (1..4), whether it claims the next
+ * batch of items before starting the current one, and the item-list lag
+ * (items listed between an image's pass and its next pass; 0 keeps the
+ * current order, whose lag is one resident grid).
+ */
+GLSFFT_API int glsfft_batch_set_schedule(glsfft_batch plan, int claim_chunk, int claim_ahead,
+                                         int lag_items);
+
+/*
+ * Synchronise `stream` and return the device-side status of the last
+ * execution: GLSFFT_SUCCESS, or GLSFFT_ERROR_TIMEOUT when a dependency wait
+ * hit its deadline (the launch still ran to completion).
+ */
+GLSFFT_API int glsfft_batch_status(glsfft_batch plan, void *stream);
+
+/* Images in the persistent launch, work items, and its grid size. */
+GLSFFT_API int glsfft_batch_info(glsfft_batch plan, int *persistent_images, int *items,
+                                 int *grid);
+
+/*
+ * Host-side fault injection for tests: make the last work item wait for one
+ * tile more than exists and set the wait deadline to wait_limit_ns, so the
+ * next execution reports GLSFFT_ERROR_TIMEOUT instead of finishing cleanly.
+ */
+GLSFFT_API int glsfft_batch_inject_stall(glsfft_batch plan, long long wait_limit_ns);
+
+GLSFFT_API int glsfft_batch_destroy(glsfft_batch plan);
+
 /*
  * gls::phaseCorrelate(src1, src2, window, &response),
  * glsCV/glsPhaseCorrelate.h:58 / glsPhaseCorrelate.cpp:142-236.

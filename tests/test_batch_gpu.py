@@ -1,0 +1,114 @@
+"""Batch plans (persistent work-queue kernel + CUDA graph) on the GPU.
+
+Each image of an uneven batch must come out bit-identical to the
+single-image gls::fft path (the persistent kernel runs the same line FFTs),
+including images routed outside the persistent launch.  Failure detection
+is tested without a GPU fault: a host-injected impossible dependency makes
+one bounded wait expire; the launch finishes and reports TIMEOUT.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import glscv_gb300 as g
+from glscv_gb300 import workloads as wl
+from tests.gpu_util import gpu_fft
+
+pytestmark = pytest.mark.gpu
+
+INV, SCALE, SHIFT = 1, 2, 64
+
+
+def _run_batch(ctx, torch, shapes, flags, seed0=700, inplace=False, variant=None):
+    xs = [wl.complex_uniform(r, c, seed0 + i) for i, (r, c) in enumerate(shapes)]
+    d_in = [torch.from_numpy(x).cuda() for x in xs]
+    d_out = d_in if inplace else [torch.empty_like(d) for d in d_in]
+    s = torch.cuda.current_stream().cuda_stream
+    b = g.Batch(ctx, [d.data_ptr() for d in d_in], [d.data_ptr() for d in d_out], shapes, flags)
+    if variant is not None:
+        b.set_variant(variant)
+    b.execute(s)
+    assert b.status(s) == 0
+    outs = [d.cpu().numpy() for d in d_out]
+    return b, xs, d_in, d_out, outs
+
+
+def _single(ctx, torch, x, flags):
+    y = x
+    for f in flags:
+        y = gpu_fft(ctx, torch, y, f)
+    return y
+
+
+@pytest.mark.parametrize("variant", [0, 1, 2])
+@pytest.mark.parametrize("flags", [(0,), (0, INV | SCALE), (SHIFT,), (INV, SCALE | SHIFT)])
+def test_uneven_batch_bit_identical_to_single_path(ctx, torch_cuda, flags, variant):
+    torch = torch_cuda
+    shapes = [(128, 128), (256, 256), (512, 512), (1024, 1024), (1024, 2048), (128, 128),
+              (16, 4096), (64, 32), (2048, 64), (1, 256), (256, 1), (4096, 4096)]
+    b, xs, _, _, outs = _run_batch(ctx, torch, shapes, flags, variant=variant)
+    info = b.info()
+    assert info["persistent_images"] == 8 and info["items"] > 0 and info["grid"] > 0
+    for i, x in enumerate(xs):
+        ref = _single(ctx, torch, x, flags)
+        assert np.array_equal(outs[i].view(np.uint32), ref.view(np.uint32)), (i, shapes[i])
+    b.close()
+
+
+def test_config3_batch_vs_oracle_and_replay(ctx, torch_cuda, oracle):
+    """64 images drawn like the 512-image configuration (seed 3), forward
+    only: each vs the oracle at the reference test's bar; the graph replays
+    to identical results."""
+    torch = torch_cuda
+    shapes = wl.batch_sizes(64, seed=3)
+    b, xs, d_in, d_out, outs = _run_batch(ctx, torch, shapes, (0,))
+    for i in range(0, 64, 9):
+        r, c = shapes[i]
+        ref = oracle.fft2d(xs[i], 0, 1)
+        assert oracle.are_equal(ref, outs[i], 64, oracle.fft_eps(max(r, c), 0) * 2) == 0
+        assert oracle.rel_l2(outs[i], oracle.fft2d_f64(xs[i])) < 1e-6
+    s = torch.cuda.current_stream().cuda_stream
+    b.execute(s)
+    assert b.status(s) == 0
+    for i in range(64):
+        assert np.array_equal(d_out[i].cpu().numpy().view(np.uint32), outs[i].view(np.uint32))
+    b.close()
+
+
+@pytest.mark.parametrize("variant", [0, 1, 2])
+def test_inplace_round_trip_batch(ctx, torch_cuda, oracle, variant):
+    torch = torch_cuda
+    shapes = [(1024, 1024)] * 6 + [(256, 512)] * 5
+    b, xs, _, _, outs = _run_batch(ctx, torch, shapes, (0, INV | SCALE), inplace=True,
+                                   variant=variant)
+    for i, x in enumerate(xs):
+        assert oracle.rel_l2(outs[i], x) < 1e-6
+    b.close()
+
+
+@pytest.mark.parametrize("variant", [0, 1, 2])
+def test_injected_stall_times_out_and_context_survives(ctx, torch_cuda, oracle, variant):
+    torch = torch_cuda
+    shapes = [(256, 256)] * 4
+    b, xs, _, d_out, _ = _run_batch(ctx, torch, shapes, (0, INV | SCALE), variant=variant)
+    b.inject_stall(50_000_000)  # 50 ms deadline on a wait that can never be met
+    s = torch.cuda.current_stream().cuda_stream
+    b.execute(s)
+    assert b.status(s) == 8  # GLSFFT_ERROR_TIMEOUT
+    b.close()
+    # the context and device still work
+    x = wl.complex_uniform(64, 64, 1)
+    y = gpu_fft(ctx, torch, x, 0)
+    assert oracle.rel_l2(y, oracle.fft2d_f64(x)) < 1e-6
+
+
+def test_batch_argument_errors(ctx, torch_cuda):
+    torch = torch_cuda
+    d = torch.zeros((8, 8), dtype=torch.complex64, device="cuda")
+    with pytest.raises(g.GlsError):
+        g.Batch(ctx, [d.data_ptr()], [d.data_ptr()], [(8, 6)], (0,))
+    with pytest.raises(g.GlsError):
+        g.Batch(ctx, [d.data_ptr()], [d.data_ptr()], [(8, 8)], (0, 1, 2))
+    with pytest.raises(g.GlsError):
+        g.Batch(ctx, [d.data_ptr()], [d.data_ptr()], [(8, 8)], (4,))
