@@ -26,7 +26,7 @@ struct glsfft_batch_s {
     int n_images = 0;      // images in the persistent launch
     int n_items = 0;
     int grid = 0;
-    int variant = BATCH_TMA_WS1;
+    int variant = BATCH_TMA_WS2;   // the fastest schedule measured on GB300
     void *d_mem = nullptr;  // tensor maps | images | passes | items | head, done, error
     BatchArgs args{};
     std::vector<BatchImage> images;
@@ -45,6 +45,12 @@ struct glsfft_batch_s {
 };
 
 namespace {
+
+// Default schedule: two warp-specialised blocks per SM, items claimed two at
+// a time, an image's next pass listed four resident grids after its previous
+// one (glsfft_batch_set_schedule / the autotuner can change all three).
+constexpr int kDefaultClaimChunk = 2;
+constexpr int kDefaultLagGrids = 4;
 
 int row_tiles_of(int rows, int cols) {
     const int lines = kBatchTileElems / cols;
@@ -238,7 +244,7 @@ int glsfft_batch_create(glsfft_context ctx, int count, const void *const *srcs,
         plan->grid = grid_for(ctx->device, plan->variant);
         if (plan->grid <= 0) st = GLSFFT_ERROR_CUDA;
         std::vector<BatchItem> items;
-        if (!st) items = order_items(plan->images, plan->passes, plan->grid);
+        if (!st) items = order_items(plan->images, plan->passes, kDefaultLagGrids * plan->grid);
         plan->n_items = (int)items.size();
         const size_t ni = plan->images.size();
         const size_t b_tm = 128 * ni;
@@ -280,7 +286,7 @@ int glsfft_batch_create(glsfft_context ctx, int count, const void *const *srcs,
             a.error = reinterpret_cast<int *>(a.done + ni * kBatchMaxPasses);
             a.tw = ctx->d_tw;
             a.wait_limit_ns = plan->wait_limit_ns;
-            a.claim_chunk = 1;
+            a.claim_chunk = kDefaultClaimChunk;
             a.claim_ahead = 0;
         }
     }
@@ -305,7 +311,8 @@ int glsfft_batch_set_variant(glsfft_batch plan, int variant) {
         if (grid <= 0) return GLSFFT_ERROR_CUDA;
         if (grid != plan->grid) {
             // the item order's lag follows the resident grid
-            std::vector<BatchItem> items = order_items(plan->images, plan->passes, grid);
+            std::vector<BatchItem> items =
+                order_items(plan->images, plan->passes, kDefaultLagGrids * grid);
             cudaError_t e = cudaMemcpy(static_cast<char *>(plan->d_mem) + plan->o_items,
                                        items.data(), sizeof(BatchItem) * items.size(),
                                        cudaMemcpyHostToDevice);

@@ -65,21 +65,12 @@ __device__ __forceinline__ void batch_rows_tile(const BatchImage &im, const Batc
     const bool cin = ps.flags & PF_CONJ_IN, cout = ps.flags & PF_CONJ_OUT;
     float2 x[E];
 #pragma unroll
-    for (int m = 0; m < E; m++) {
-        float2 v = active ? load_c2<FIRST>(src + (size_t)row * N + t + m * T) : make_float2(0.f, 0.f);
-        x[m] = cin ? cconj(v) : v;
-    }
-    LineFft<N, E>::run(x, t, RowSm{smem + l * padded_count(N)}, tw + N);
-    const float s = ps.scale ? 1.0f / (float)N : 1.0f;
-    const bool shift = ps.flags & PF_SHIFT_COLS;
-#pragma unroll
-    for (int m = 0; m < E; m++) {
-        const int pos = t + m * T;
-        const int ocol = shift ? (pos + (N >> 1)) & (N - 1) : pos;
-        float2 v = cscale(x[m], s);
-        if (cout) v = cconj(v);
-        if (active) im.dst[(size_t)row * N + ocol] = v;
-    }
+    for (int m = 0; m < E; m++)
+        x[m] = active ? load_c2<FIRST>(src + (size_t)row * N + t + m * T) : make_float2(0.f, 0.f);
+    conj_line(x, cin);
+    LineFft<N, E>::run(x, t, RowSm{smem + l * padded_count(N)}, tw);
+    finish_line(x, ps.scale ? 1.0f / (float)N : 1.0f, cout);
+    if (active) store_line<N, E, T>(im.dst + (size_t)row * N, 1, x, t, ps.flags & PF_SHIFT_COLS);
 }
 
 template <int N, bool FIRST>
@@ -94,21 +85,12 @@ __device__ __forceinline__ void batch_cols_tile(const BatchImage &im, const Batc
     const bool cin = ps.flags & PF_CONJ_IN, cout = ps.flags & PF_CONJ_OUT;
     float2 x[E];
 #pragma unroll
-    for (int m = 0; m < E; m++) {
-        float2 v = active ? load_c2<FIRST>(src + (size_t)(t + m * T) * cols + col) : make_float2(0.f, 0.f);
-        x[m] = cin ? cconj(v) : v;
-    }
-    LineFft<N, E>::run(x, t, ColSm<W>{smem, c}, tw + N);
-    const float s = ps.scale ? 1.0f / (float)N : 1.0f;
-    const bool shift = ps.flags & PF_SHIFT_ROWS;
-#pragma unroll
-    for (int m = 0; m < E; m++) {
-        const int pos = t + m * T;
-        const int orow = shift ? (pos + (N >> 1)) & (N - 1) : pos;
-        float2 v = cscale(x[m], s);
-        if (cout) v = cconj(v);
-        if (active) im.dst[(size_t)orow * cols + col] = v;
-    }
+    for (int m = 0; m < E; m++)
+        x[m] = active ? load_c2<FIRST>(src + (size_t)(t + m * T) * cols + col) : make_float2(0.f, 0.f);
+    conj_line(x, cin);
+    LineFft<N, E>::run(x, t, ColSm<W>{smem, c}, tw);
+    finish_line(x, ps.scale ? 1.0f / (float)N : 1.0f, cout);
+    if (active) store_line<N, E, T>(im.dst + col, (size_t)cols, x, t, ps.flags & PF_SHIFT_ROWS);
 }
 
 template <bool FIRST>

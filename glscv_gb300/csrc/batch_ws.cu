@@ -81,16 +81,24 @@ __device__ __forceinline__ bool mbar_test(unsigned long long *b, unsigned parity
         : "memory");
     return ok != 0;
 }
+// One try_wait: the thread may be suspended (not spinning on issue slots)
+// until the phase completes or a hardware time limit passes.
+__device__ __forceinline__ bool mbar_try(unsigned long long *b, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(b)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
 // Bounded wait for the phase with `parity` to complete; false on expiry.
 __device__ bool mbar_wait(unsigned long long *b, unsigned parity, long long limit_ns) {
-    if (mbar_test(b, parity)) return true;
+    if (mbar_try(b, parity)) return true;
     const unsigned long long t0 = gtimer();
-    for (unsigned it = 0; it < (1u << 26); it++) {
-        if (mbar_test(b, parity)) return true;
-        if ((it & 63) == 63) {
-            if ((long long)(gtimer() - t0) > limit_ns) return false;
-            __nanosleep(64);
-        }
+    for (unsigned it = 0; it < (1u << 24); it++) {
+        if (mbar_try(b, parity)) return true;
+        if ((long long)(gtimer() - t0) > limit_ns) return false;
     }
     return false;
 }
@@ -126,23 +134,14 @@ __device__ __forceinline__ void ws_rows(float2 *stage, const StageInfo &in, cons
     const bool active = row < in.rows;
     const bool cin = in.flags & PF_CONJ_IN, cout = in.flags & PF_CONJ_OUT;
     float2 x[E];
+    const float2 *sp = stage + l * N + t;
 #pragma unroll
-    for (int m = 0; m < E; m++) {
-        float2 v = active ? stage[l * N + t + m * T] : make_float2(0.f, 0.f);
-        x[m] = cin ? cconj(v) : v;
-    }
+    for (int m = 0; m < E; m++) x[m] = active ? sp[m * T] : make_float2(0.f, 0.f);
+    conj_line(x, cin);
     SyncCompute256{}();  // the exchanges below overwrite the staged tile
-    LineFft<N, E, SyncCompute256>::run(x, t, RowSm{stage + l * padded_count(N)}, tw + N);
-    const float s = in.scale ? 1.0f / (float)N : 1.0f;
-    const bool shift = in.flags & PF_SHIFT_COLS;
-#pragma unroll
-    for (int m = 0; m < E; m++) {
-        const int pos = t + m * T;
-        const int ocol = shift ? (pos + (N >> 1)) & (N - 1) : pos;
-        float2 v = cscale(x[m], s);
-        if (cout) v = cconj(v);
-        if (active) in.dst[(size_t)row * N + ocol] = v;
-    }
+    LineFft<N, E, SyncCompute256>::run(x, t, RowSm{stage + l * padded_count(N)}, tw);
+    finish_line(x, in.scale ? 1.0f / (float)N : 1.0f, cout);
+    if (active) store_line<N, E, T>(in.dst + (size_t)row * N, 1, x, t, in.flags & PF_SHIFT_COLS);
 }
 
 template <int N>
@@ -154,23 +153,14 @@ __device__ __forceinline__ void ws_cols(float2 *stage, const StageInfo &in, cons
     const bool active = col < in.cols;
     const bool cin = in.flags & PF_CONJ_IN, cout = in.flags & PF_CONJ_OUT;
     float2 x[E];
+    const float2 *sp = stage + t * W + c;  // out-of-range columns were zero-filled
 #pragma unroll
-    for (int m = 0; m < E; m++) {
-        float2 v = stage[(t + m * T) * W + c];  // out-of-range columns were zero-filled
-        x[m] = cin ? cconj(v) : v;
-    }
+    for (int m = 0; m < E; m++) x[m] = sp[m * T * W];
+    conj_line(x, cin);
     SyncCompute256{}();
-    LineFft<N, E, SyncCompute256>::run(x, t, ColSm<W>{stage, c}, tw + N);
-    const float s = in.scale ? 1.0f / (float)N : 1.0f;
-    const bool shift = in.flags & PF_SHIFT_ROWS;
-#pragma unroll
-    for (int m = 0; m < E; m++) {
-        const int pos = t + m * T;
-        const int orow = shift ? (pos + (N >> 1)) & (N - 1) : pos;
-        float2 v = cscale(x[m], s);
-        if (cout) v = cconj(v);
-        if (active) in.dst[(size_t)orow * in.cols + col] = v;
-    }
+    LineFft<N, E, SyncCompute256>::run(x, t, ColSm<W>{stage, c}, tw);
+    finish_line(x, in.scale ? 1.0f / (float)N : 1.0f, cout);
+    if (active) store_line<N, E, T>(in.dst + col, (size_t)in.cols, x, t, in.flags & PF_SHIFT_ROWS);
 }
 
 __device__ __forceinline__ void ws_compute(float2 *stage, const StageInfo &in, const float2 *tw, int tid) {

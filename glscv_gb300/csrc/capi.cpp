@@ -16,39 +16,49 @@
 using namespace glsfft;
 
 // --------------------------------------------------------------- twiddles
-// e^{-2 pi i k/n}, k < n, from an exact quadrant / octant reduction so that
-// +-1, 0 and the pi/4 values come out exact and symmetric; FP64, then one
-// rounding to FP32.
-void glsfft::make_twiddle_host(float2 *dst) {
+// e^{-2 pi i k/n} (k < n, n a power of two) in FP64 from an exact quadrant /
+// octant reduction, so that +-1, 0 and the pi/4 values come out exact and
+// symmetric, then one rounding to FP32.
+static float2 twiddle(long long k, long long n) {
     const double two_pi = 6.283185307179586476925286766559;
-    for (int n = 2; n <= kMaxLen; n <<= 1) {
-        for (int k = 0; k < n; k++) {
-            const int q = (4 * k) / n;        // quadrant
-            const int r = k - q * (n / 4);    // position inside the quadrant
-            double c, s;                      // cos, sin of 2 pi r / n
-            if (n < 4) {
-                c = (k == 0) ? 1.0 : -1.0;
-                s = 0.0;
-            } else if (8 * r <= n) {
-                c = std::cos(two_pi * r / n);
-                s = std::sin(two_pi * r / n);
-            } else {
-                const double a = two_pi * (n / 4 - r) / n;
-                c = std::sin(a);
-                s = std::cos(a);
-            }
-            double cr = c, sr = s;  // rotate by i^q
-            if (n >= 4) {
-                for (int i = 0; i < q; i++) {
-                    const double t = cr;
-                    cr = -sr;
-                    sr = t;
-                }
-            }
-            // forward sign: e^{-i theta} = cos - i sin
-            dst[n + k] = make_float2((float)cr, (float)(-sr));
-        }
+    k %= n;
+    if (n < 4) return make_float2(k == 0 ? 1.0f : -1.0f, 0.0f);
+    const long long q = (4 * k) / n;       // quadrant
+    const long long r = k - q * (n / 4);   // position inside the quadrant
+    double c, s;                           // cos, sin of 2 pi r / n
+    if (8 * r <= n) {
+        c = std::cos(two_pi * (double)r / (double)n);
+        s = std::sin(two_pi * (double)r / (double)n);
+    } else {
+        const double a = two_pi * (double)(n / 4 - r) / (double)n;
+        c = std::sin(a);
+        s = std::cos(a);
     }
+    for (long long i = 0; i < q; i++) {  // rotate by i^q
+        const double t = c;
+        c = -s;
+        s = t;
+    }
+    return make_float2((float)c, (float)(-s));  // forward sign: cos - i sin
+}
+
+// Per-pass tables (see tw_offset), for every radix R and every length
+// R <= L <= kTwRadixSpan / 2: row k < L/R of table (R, L) holds
+// w^r = e^{-2 pi i k r / L} for 1 <= r < R/2 in slot r and w^(R/2) in slot 0
+// (the line engine derives w^(R/2+r) = w^(R/2) w^r); for R = 2 slot 0 holds w^1.
+void glsfft::make_twiddle_host(float2 *dst) {
+    for (int i = 0; i < kTwEntries; i++) dst[i] = make_float2(0.f, 0.f);
+    for (int radix = 2; radix <= 16; radix <<= 1)
+        for (int l = radix; l <= kTwRadixSpan / 2; l <<= 1)
+            for (int k = 0; k < l / radix; k++) {
+                float2 *row = dst + tw_offset(radix, l) + k * radix;
+                if (radix == 2) {
+                    row[0] = twiddle(k, l);
+                    continue;
+                }
+                row[0] = twiddle((long long)k * (radix / 2), l);
+                for (int r = 1; r < radix / 2; r++) row[r] = twiddle((long long)k * r, l);
+            }
 }
 
 // ---------------------------------------------------------------- helpers
@@ -119,7 +129,7 @@ int glsfft::fft2d_launch(glsfft_context ctx, const void *src, void *dst, int row
         a.scale = scale ? 1.0f / (float)cols : 1.0f;
         a.flags = (inv ? PF_CONJ_IN : 0u) | (inv && !do_cols ? PF_CONJ_OUT : 0u) |
                   (shift ? PF_SHIFT_COLS : 0u);
-        a.tw = ctx->d_tw + cols;
+        a.tw = ctx->d_tw;
         a.in_img_bytes = px * (real_in ? sizeof(float) : sizeof(float2));
         a.out_img_bytes = px * sizeof(float2);
         cudaError_t e = launch_rows(cols, real_in ? LD_R1 : LD_C2, ST_C2, a, count, s);
@@ -134,7 +144,7 @@ int glsfft::fft2d_launch(glsfft_context ctx, const void *src, void *dst, int row
         a.scale = scale ? 1.0f / (float)rows : 1.0f;
         a.flags = (inv && !do_rows ? PF_CONJ_IN : 0u) | (inv ? PF_CONJ_OUT : 0u) |
                   (shift ? PF_SHIFT_ROWS : 0u);
-        a.tw = ctx->d_tw + rows;
+        a.tw = ctx->d_tw;
         a.in_img_bytes = a.out_img_bytes = px * sizeof(float2);
         cudaError_t e = launch_cols(rows, LD_C2, ST_C2, a, count, s);
         if (e != cudaSuccess) return cuda_status(e);
@@ -159,7 +169,7 @@ int glsfft::poc_launch(const float2 *tw, const float *src1, const float *src2,
     a.rows = rows;
     a.cols = cols;
     a.scale = 1.0f;
-    a.tw = tw + cols;
+    a.tw = tw;
     e = launch_rows(cols, window ? LD_R1W : LD_R1, ST_C2, a, 2, s);
     if (e != cudaSuccess) return cuda_status(e);
 
@@ -170,7 +180,7 @@ int glsfft::poc_launch(const float2 *tw, const float *src1, const float *src2,
     b.rows = rows;
     b.cols = cols;
     b.scale = 1.0f;
-    b.tw = tw + rows;
+    b.tw = tw;
     e = launch_poc_cols(rows, b, s);
     if (e != cudaSuccess) return cuda_status(e);
 
@@ -182,7 +192,7 @@ int glsfft::poc_launch(const float2 *tw, const float *src1, const float *src2,
     c.scale = 1.0f;
     c.flags = PF_SHIFT_ROWS | PF_SHIFT_COLS;
     c.key = key;
-    c.tw = tw + cols;
+    c.tw = tw;
     e = launch_rows(cols, LD_C2, ST_RE_ARGMAX, c, 1, s);
     if (e != cudaSuccess) return cuda_status(e);
 
@@ -251,7 +261,7 @@ int glsfft_context_create(glsfft_context *out, int device) {
     auto *ctx = new (std::nothrow) glsfft_context_s();
     if (!ctx) return GLSFFT_ERROR_OUT_OF_MEMORY;
     ctx->device = device;
-    std::vector<float2> tw(2 * (size_t)kMaxLen);
+    std::vector<float2> tw((size_t)kTwEntries);
     make_twiddle_host(tw.data());
     e = cudaMalloc(&ctx->d_tw, sizeof(float2) * tw.size());
     if (e == cudaSuccess)
@@ -327,7 +337,7 @@ static int one_pass(glsfft_context ctx, const void *src, void *dst, int count, i
     a.scale = (flags & GLSFFT_SCALE) ? 1.0f / (float)n : 1.0f;
     a.flags = (inv ? PF_CONJ_IN | PF_CONJ_OUT : 0u) |
               ((flags & GLSFFT_SHIFT) ? (along_rows ? PF_SHIFT_COLS : PF_SHIFT_ROWS) : 0u);
-    a.tw = ctx->d_tw + n;
+    a.tw = ctx->d_tw;
     a.in_img_bytes = a.out_img_bytes = (size_t)rows * cols * sizeof(float2);
     cudaError_t e = along_rows ? launch_rows(n, LD_C2, ST_C2, a, count, s)
                                : launch_cols(n, LD_C2, ST_C2, a, count, s);

@@ -20,6 +20,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "glsfft_internal.h"
+
 namespace glsfft {
 
 // ------------------------------------------------------------ complex helpers
@@ -145,8 +147,24 @@ struct SyncCompute256 {
     }
 };
 
-// Sm: shared-memory accessor, sm(pos) -> float2& for this thread's line.
-// tw: twiddle table for length N, tw[k] = e^{-2 pi i k/N}, k < N.
+// Shared-memory accessors map a line position to a padded slot: the linear
+// index i (position * KW + column) gets one pad per 16, slot = i + i/16.
+// Strided<Sm, DELTA, COUNT> tells whether COUNT accesses DELTA positions
+// apart from a base are a fixed slot step apart (so one address and
+// compile-time offsets serve them all): true when the linear step is a
+// multiple of 16, or when all COUNT accesses fall inside one 16-slot block
+// (the base is then aligned to DELTA*COUNT*KW, as every caller's base is).
+template <class Sm, int DELTA, int COUNT>
+struct Strided {
+    static constexpr int LIN = DELTA * Sm::KW;
+    static constexpr bool by_block = (LIN % 16) == 0;
+    static constexpr bool in_block = LIN * COUNT <= 16;
+    static constexpr bool affine = by_block || in_block;
+    static constexpr int STEP = by_block ? LIN + LIN / 16 : LIN;
+};
+
+// Sm: shared-memory accessor (at(pos) -> float2*, KW) for this thread's line.
+// tw: the per-pass twiddle tables above.
 template <int N, int E, class Sync = SyncBlock>
 struct LineFft {
     static_assert((N & (N - 1)) == 0 && N >= 1 && N <= 8192, "N must be a power of two");
@@ -177,10 +195,31 @@ struct LineFft {
 #pragma unroll
                 for (int r = 0; r < R; r++) v[r] = x[s + r * S];
                 if constexpr (Ns > 1) {
+                    // w^0..w^(R/2-1) come from the table (R/4 16-byte loads);
+                    // w^(R/2+r) = w^(R/2) * w^r, one extra rounding, halves
+                    // the twiddle loads (entry R/2 is stored in slot 0, whose
+                    // value w^0 = 1 is never needed)
                     const int k = j & (Ns - 1);
-                    constexpr int step = N / (Ns * R);
+                    const float2 *wt = tw + tw_offset(R, Ns * R) + k * R;
+                    if constexpr (R == 2) {
+                        v[1] = cmul(v[1], __ldg(wt));
+                    } else {
+                        float2 w[R / 2];
+                        const float4 *w4 = reinterpret_cast<const float4 *>(wt);
 #pragma unroll
-                    for (int r = 1; r < R; r++) v[r] = cmul(v[r], __ldg(tw + k * r * step));
+                        for (int h = 0; h < R / 4; h++) {
+                            const float4 q = __ldg(w4 + h);
+                            w[2 * h] = make_float2(q.x, q.y);
+                            w[2 * h + 1] = make_float2(q.z, q.w);
+                        }
+                        const float2 wh = w[0];  // w^(R/2)
+#pragma unroll
+                        for (int r = 1; r < R / 2; r++) {
+                            v[r] = cmul(v[r], w[r]);
+                            v[r + R / 2] = cmul(v[r + R / 2], cmul(wh, w[r]));
+                        }
+                        v[R / 2] = cmul(v[R / 2], wh);
+                    }
                 }
                 Dft<R>::run(v);
                 if constexpr (last) {
@@ -188,14 +227,28 @@ struct LineFft {
                     for (int r = 0; r < R; r++) x[s + r * S] = v[r];
                 } else {
                     const int d = (j / Ns) * Ns * R + (j & (Ns - 1));
+                    using WS = Strided<Sm, Ns, R>;
+                    if constexpr (WS::affine) {
+                        float2 *o = sm.at(d);
 #pragma unroll
-                    for (int r = 0; r < R; r++) sm(d + r * Ns) = v[r];
+                        for (int r = 0; r < R; r++) o[r * WS::STEP] = v[r];
+                    } else {
+#pragma unroll
+                        for (int r = 0; r < R; r++) *sm.at(d + r * Ns) = v[r];
+                    }
                 }
             }
             if constexpr (!last) {
                 sync();
+                using RS = Strided<Sm, T, E>;
+                if constexpr (RS::affine) {
+                    const float2 *in = sm.at(t);
 #pragma unroll
-                for (int m = 0; m < E; m++) x[m] = sm(t + m * T);
+                    for (int m = 0; m < E; m++) x[m] = in[m * RS::STEP];
+                } else {
+#pragma unroll
+                    for (int m = 0; m < E; m++) x[m] = *sm.at(t + m * T);
+                }
                 sync();
                 pass<p + 1>(x, t, sm, tw);
             }

@@ -23,20 +23,57 @@ namespace glsfft {
 // values keeps the stride-R butterfly writes of the first exchange on
 // distinct banks.
 struct RowSm {
+    static constexpr int KW = 1;
     float2 *base;
-    __device__ __forceinline__ float2 &operator()(int pos) const { return base[pos + (pos >> 4)]; }
+    __device__ __forceinline__ float2 *at(int pos) const { return base + pos + (pos >> 4); }
 };
 // Column tiles keep [position][column] order (like the image) with the same
 // per-16 padding over the linearised index.
 template <int W>
 struct ColSm {
+    static constexpr int KW = W;
     float2 *base;
     int c;
-    __device__ __forceinline__ float2 &operator()(int pos) const {
+    __device__ __forceinline__ float2 *at(int pos) const {
         const int i = pos * W + c;
-        return base[i + (i >> 4)];
+        return base + i + (i >> 4);
     }
 };
+
+// Whole-line conjugation and scaling behind uniform branches, so the common
+// flag-free case spends no instructions per element.
+template <int E>
+__device__ __forceinline__ void conj_line(float2 (&x)[E], bool on) {
+    if (on) {
+#pragma unroll
+        for (int m = 0; m < E; m++) x[m].y = -x[m].y;
+    }
+}
+template <int E>
+__device__ __forceinline__ void finish_line(float2 (&x)[E], float scale, bool conj_out) {
+    if (scale != 1.0f) {
+        const float si = conj_out ? -scale : scale;
+#pragma unroll
+        for (int m = 0; m < E; m++) x[m] = make_float2(x[m].x * scale, x[m].y * si);
+    } else {
+        conj_line(x, conj_out);
+    }
+}
+
+// Store a line held as x[m] = position t + m*T, optionally half-swapped
+// (fftshift along the line): dst + pos*STRIDE for each position pos.
+template <int N, int E, int T>
+__device__ __forceinline__ void store_line(float2 *dst, size_t stride, const float2 (&x)[E],
+                                           int t, bool shift) {
+    if (shift) {
+#pragma unroll
+        for (int m = 0; m < E; m++) dst[(size_t)((t + m * T + (N >> 1)) & (N - 1)) * stride] = x[m];
+    } else {
+        float2 *p = dst + (size_t)t * stride;
+#pragma unroll
+        for (int m = 0; m < E; m++) p[(size_t)m * T * stride] = x[m];
+    }
+}
 
 // Image z of a launch: in1/out1 when set (the two-image phaseCorrelate
 // launch), else image z of a contiguous batch starting at in0/out0.
@@ -84,32 +121,32 @@ __global__ void __launch_bounds__(LINES *LineFft<N, E>::T)
 #pragma unroll
     for (int m = 0; m < E; m++) {
         const int pos = t + m * T;
-        float2 v = active ? load_elem<LD>(in, a.window, (size_t)row * N + pos) : make_float2(0.f, 0.f);
-        x[m] = conj_in ? cconj(v) : v;
+        x[m] = active ? load_elem<LD>(in, a.window, (size_t)row * N + pos) : make_float2(0.f, 0.f);
     }
+    conj_line(x, conj_in);
     F::run(x, t, RowSm{smem + l * padded_count(N)}, a.tw);
 
     const int orow = (a.flags & PF_SHIFT_ROWS) ? (row + (a.rows >> 1)) & (a.rows - 1) : row;
-    const bool conj_out = a.flags & PF_CONJ_OUT;
-    unsigned long long best = 0;
+    finish_line(x, a.scale, a.flags & PF_CONJ_OUT);
+    if constexpr (ST == ST_C2) {
+        if (active)
+            store_line<N, E, T>(reinterpret_cast<float2 *>(out) + (size_t)orow * N, 1, x, t,
+                                a.flags & PF_SHIFT_COLS);
+    } else {
+        unsigned long long best = 0;
 #pragma unroll
-    for (int m = 0; m < E; m++) {
-        const int pos = t + m * T;
-        const int ocol = (a.flags & PF_SHIFT_COLS) ? (pos + (N >> 1)) & (N - 1) : pos;
-        float2 v = cscale(x[m], a.scale);
-        if (conj_out) v = cconj(v);
-        const size_t o = (size_t)orow * N + ocol;
-        if constexpr (ST == ST_C2) {
-            if (active) reinterpret_cast<float2 *>(out)[o] = v;
-        } else {
-            if (active) reinterpret_cast<float *>(out)[o] = v.x;
+        for (int m = 0; m < E; m++) {
+            const int pos = t + m * T;
+            const int ocol = (a.flags & PF_SHIFT_COLS) ? (pos + (N >> 1)) & (N - 1) : pos;
+            const size_t o = (size_t)orow * N + ocol;
+            if (active) reinterpret_cast<float *>(out)[o] = x[m].x;
             if constexpr (ST == ST_RE_ARGMAX) {
-                unsigned long long k = active ? argmax_key(v.x, (unsigned)o) : 0ull;
+                unsigned long long k = active ? argmax_key(x[m].x, (unsigned)o) : 0ull;
                 best = k > best ? k : best;
             }
         }
+        if constexpr (ST == ST_RE_ARGMAX) block_argmax_commit(best, red, a.key);
     }
-    if constexpr (ST == ST_RE_ARGMAX) block_argmax_commit(best, red, a.key);
 }
 
 // ---------------------------------------------------------- column pass
@@ -134,26 +171,17 @@ __global__ void __launch_bounds__(W *LineFft<N, E>::T)
 #pragma unroll
     for (int m = 0; m < E; m++) {
         const int pos = t + m * T;
-        float2 v = active ? load_elem<LD>(in, a.window, (size_t)pos * cols + col) : make_float2(0.f, 0.f);
-        x[m] = conj_in ? cconj(v) : v;
+        x[m] = active ? load_elem<LD>(in, a.window, (size_t)pos * cols + col) : make_float2(0.f, 0.f);
     }
+    conj_line(x, conj_in);
     F::run(x, t, ColSm<W>{smem, c}, a.tw);
 
     const int ocol = (a.flags & PF_SHIFT_COLS) ? (col + (cols >> 1)) & (cols - 1) : col;
-    const bool conj_out = a.flags & PF_CONJ_OUT;
-#pragma unroll
-    for (int m = 0; m < E; m++) {
-        const int pos = t + m * T;
-        const int orow = (a.flags & PF_SHIFT_ROWS) ? (pos + (N >> 1)) & (N - 1) : pos;
-        float2 v = cscale(x[m], a.scale);
-        if (conj_out) v = cconj(v);
-        const size_t o = (size_t)orow * cols + ocol;
-        if constexpr (ST == ST_C2) {
-            if (active) reinterpret_cast<float2 *>(out)[o] = v;
-        } else {
-            if (active) reinterpret_cast<float *>(out)[o] = v.x;
-        }
-    }
+    finish_line(x, a.scale, a.flags & PF_CONJ_OUT);
+    static_assert(ST == ST_C2, "the column pass stores complex values");
+    if (active)
+        store_line<N, E, T>(reinterpret_cast<float2 *>(out) + ocol, (size_t)cols, x, t,
+                            a.flags & PF_SHIFT_ROWS);
 }
 
 // --------------------------------------------- fused phaseCorrelate columns

@@ -9,6 +9,19 @@ namespace glsfft {
 
 constexpr int kMaxLen = 4096;  // largest supported FFT length per dimension
 
+// Per-pass twiddle tables: for a pass of radix R whose sub-transforms have
+// length L (= span * R), entry [k][r] = e^{-2 pi i k r / L}, k < L/R, r < R,
+// so a butterfly fetches its R twiddles with R/2 16-byte loads.  All tables
+// live in one buffer of kTwEntries float2, table (R, L) at tw_offset(R, L).
+constexpr int kTwRadixSpan = 8192;
+constexpr int kTwEntries = 4 * kTwRadixSpan;
+__host__ __device__ constexpr int tw_radix_index(int r) {
+    return r == 2 ? 0 : r == 4 ? 1 : r == 8 ? 2 : 3;
+}
+__host__ __device__ constexpr int tw_offset(int r, int l) {
+    return tw_radix_index(r) * kTwRadixSpan + l;
+}
+
 // load modes of the first pass
 enum { LD_C2 = 0, LD_R1 = 1, LD_R1W = 2 };
 // store modes of the last pass
@@ -45,9 +58,9 @@ cudaError_t launch_poc_cols(int n, const PassArgs &a, cudaStream_t s);
 cudaError_t launch_poc_finish(const float *surface, int rows, int cols, int box,
                               const unsigned long long *key, double *res, cudaStream_t s);
 
-// Twiddle tables: one device buffer, table for length n (power of two,
-// 2 <= n <= kMaxLen) at entries [n, 2n), value e^{-2 pi i k/n}.  Generated in
-// FP64 on the host and rounded once to FP32.
-void make_twiddle_host(float2 *dst /* 2*kMaxLen entries */);
+// Twiddle tables: one device buffer of kTwEntries float2 holding the
+// per-pass tables of fft_device.cuh (tw_offset).  Generated in FP64 on the
+// host and rounded once to FP32.
+void make_twiddle_host(float2 *dst /* kTwEntries entries */);
 
 }  // namespace glsfft

@@ -18,7 +18,7 @@ constexpr size_t kKeyOffset = (20 * kMaxPixels + 255) / 256 * 256;
 constexpr size_t kScratchBytes = kKeyOffset + 256;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
-static __device__ __align__(256) float2 g_noalloc_twiddles[2 * glsfft::kMaxLen];
+static __device__ __align__(256) float2 g_noalloc_twiddles[glsfft::kTwEntries];
 
 struct DeviceSetup {
     bool ready = false;
@@ -29,7 +29,7 @@ struct DeviceSetup {
 constexpr int kMaxDevices = 64;
 std::mutex g_setup_mutex;
 DeviceSetup g_setup[kMaxDevices];
-float2 g_host_twiddles[2 * glsfft::kMaxLen];  // staging for the one upload
+float2 g_host_twiddles[glsfft::kTwEntries];  // staging for the one upload
 
 // Once per device, with that device current.
 int setup_current_device(DeviceSetup **out) {

@@ -144,8 +144,8 @@ GLSFFT_API int glsfft_batch_execute(glsfft_batch plan, void *stream);
  * Persistent-kernel schedule of a plan (re-captures its graph):
  * 0 = every thread loads its own operands (2 blocks/SM);
  * 1 = warp-specialised: a producer warp stages tiles with TMA into a 3-stage
- *     shared-memory ring for 8 compute warps (1 block/SM, the default);
- * 2 = the same at 2 blocks/SM (registers capped, some spilling).
+ *     shared-memory ring for 8 compute warps (1 block/SM);
+ * 2 = the same at 2 blocks/SM (registers capped at 96; the default).
  */
 #define GLSFFT_BATCH_PLAIN 0
 #define GLSFFT_BATCH_TMA_WS1 1
@@ -157,7 +157,7 @@ GLSFFT_API int glsfft_batch_set_variant(glsfft_batch plan, int variant);
  * queue atomic by a warp-specialised block (1..4), whether it claims the next
  * batch of items before starting the current one, and the item-list lag
  * (items listed between an image's pass and its next pass; 0 keeps the
- * current order, whose lag is one resident grid).
+ * current order).  Defaults: 2, 0, four resident grids.
  */
 GLSFFT_API int glsfft_batch_set_schedule(glsfft_batch plan, int claim_chunk, int claim_ahead,
                                          int lag_items);
