@@ -45,6 +45,8 @@ def parse():
     p.add_argument("--images", type=int, default=64, help="images per step per GPU")
     p.add_argument("--cpu-sample", type=int, default=2, help="images per CPU-baseline step")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--profile-only", action="store_true",
+                   help="build the batch plan, run it warmup+1 times and exit (for ncu)")
     return p.parse_args()
 
 
@@ -281,6 +283,18 @@ def run_own(args) -> None:
         p1.record(stream)
         torch.cuda.synchronize()
         return max_over_ranks(p0.elapsed_time(p1) / k)
+
+    if args.profile_only:
+        for _ in range(args.warmup + 1):
+            step(False)
+        torch.cuda.synchronize()
+        st = plan.status(s)
+        print(json.dumps({"profile_only": True, "images": B, "status": st}), flush=True)
+        if dist is not None:
+            dist.destroy_process_group()
+        plan.close()
+        ctx.close()
+        return
 
     for _ in range(max(3, args.warmup)):
         step(False)
