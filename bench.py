@@ -45,6 +45,7 @@ def parse():
     p.add_argument("--images", type=int, default=64, help="images per step per GPU")
     p.add_argument("--cpu-sample", type=int, default=2, help="images per CPU-baseline step")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-serving", action="store_true", help="skip the serving sweep")
     p.add_argument("--profile-only", action="store_true",
                    help="build the batch plan, run it warmup+1 times and exit (for ncu)")
     return p.parse_args()
@@ -201,6 +202,71 @@ def run_reference(args) -> None:
                 "the reference's own CPU Stockham is timed instead",
     }
     print(json.dumps(line), flush=True)
+
+
+# ----------------------------------------------------------------- serving
+SERVE_SIZES = [512, 1024, 2048]
+SERVE_MIX = [0.5, 0.35, 0.15]
+SERVE_REFS = [16, 11, 5]          # 32 resident reference spectra
+SERVE_RATES = [1000, 5000, 10000, 20000, 50000]
+
+
+def serving_sweep(g, ctx, torch, seconds: float = 0.5, max_requests: int = 4000) -> dict:
+    """Poisson arrivals (seed 5) of CV_32FC1 frame pairs against 32 resident
+    reference spectra; frames are the reference shifted by a seeded integer +
+    sub-pixel amount (Fourier shift) plus N(0, 0.01^2); latency = arrival to
+    result on the host, measured natively by the server."""
+    import numpy as np
+    from glscv_gb300 import workloads as wl
+
+    rng = np.random.default_rng(5)
+    srv = g.Server(ctx, slots=8, hbm_budget=3 << 30)
+    keep, frames_by_size, refs_by_size = [], {}, {}
+    for n, count in zip(SERVE_SIZES, SERVE_REFS):
+        w = wl.hann_window(n, n)
+        dw = torch.from_numpy(w).cuda()
+        keep.append(dw)
+        base = wl.smooth_field(n, n, seed=60 + n)
+        for r in range(count):
+            a = np.roll(base, (r * 37, r * 53), axis=(0, 1))  # distinct references
+            da = torch.from_numpy(np.ascontiguousarray(a)).cuda()
+            rid = srv.add_reference(da.data_ptr(), dw.data_ptr(), n, n)
+            keep.append(da)
+            refs_by_size.setdefault(n, []).append((rid, a))
+        # two frames per size class, shifted copies of that class's first reference
+        rid0, a0 = refs_by_size[n][0]
+        for k in range(2):
+            sx = float(rng.integers(-50, 51)) + float(rng.uniform(-0.5, 0.5))
+            sy = float(rng.integers(-50, 51)) + float(rng.uniform(-0.5, 0.5))
+            fy = np.fft.fftfreq(n)[:, None]
+            fx = np.fft.fftfreq(n)[None, :]
+            b = np.real(np.fft.ifft2(np.fft.fft2(a0) * np.exp(-2j * np.pi * (fx * sx + fy * sy))))
+            b = b + rng.normal(0, 0.01, b.shape)
+            hb = torch.empty((n, n), dtype=torch.float32, pin_memory=True)
+            hb.copy_(torch.from_numpy(b.astype(np.float32)))
+            frames_by_size.setdefault(n, []).append((rid0, hb, (sx, sy)))
+    out = {"slots": 8, "hbm_budget_bytes": 3 << 30, "references": sum(SERVE_REFS),
+           "mix": dict(zip([f"{n}x{n}" for n in SERVE_SIZES], SERVE_MIX)), "rates": []}
+    for rate in SERVE_RATES:
+        n_req = int(min(max_requests, rate * seconds))
+        offs = np.cumsum(rng.exponential(1.0 / rate, n_req))
+        cls = rng.choice(len(SERVE_SIZES), size=n_req, p=SERVE_MIX)
+        pick = [frames_by_size[SERVE_SIZES[c]][int(rng.integers(0, 2))] for c in cls]
+        lat, res = srv.replay(offs, [p[0] for p in pick], [p[1].data_ptr() for p in pick])
+        lat = np.array(lat) * 1e3
+        err = max(max(abs(r[0] - p[2][0]), abs(r[1] - p[2][1])) for r, p in zip(res, pick))
+        span = offs[-1] + lat[-1] / 1e3
+        l1024 = lat[[SERVE_SIZES[c] == 1024 for c in cls]]
+        out["rates"].append({
+            "offered_per_s": rate, "requests": n_req,
+            "pairs_per_s": round(n_req / span, 1),
+            "p50_ms": round(float(np.percentile(lat, 50)), 4),
+            "p99_ms": round(float(np.percentile(lat, 99)), 4),
+            "p99_ms_1024": round(float(np.percentile(l1024, 99)), 4) if len(l1024) else None,
+            "max_shift_error_px": round(float(err), 4)})
+    out["stats"] = srv.stats()
+    srv.close()
+    return out
 
 
 # ---------------------------------------------------------------- own arm
@@ -400,6 +466,7 @@ def run_own(args) -> None:
 
     if rank == 0:
         cb = cpu_baseline(min(args.cpu_sample, B))
+        serving = None if args.no_serving else serving_sweep(g, ctx, torch)
         line = {
             "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": round(ms, 4),
@@ -422,6 +489,7 @@ def run_own(args) -> None:
             "cpu_baseline": cb,
             "e2e": e2e,
             "phase_correlate": pc,
+            "serving": serving,
             "clocks": clk,
             "gpu_launches": launches_per_step * args.steps,
         }

@@ -60,6 +60,14 @@ _SIGNATURES = {
                                 ctypes.POINTER(_ip)]),
     "glsfft_batch_inject_stall": (_ip, [_vp, ctypes.c_longlong]),
     "glsfft_batch_destroy": (_ip, [_vp]),
+    "glsfft_server_create": (_ip, [_vp, _ip, _sz, ctypes.POINTER(_vp)]),
+    "glsfft_server_add_reference": (_ip, [_vp, _vp, _vp, _ip, _ip, ctypes.POINTER(_ip)]),
+    "glsfft_server_submit": (_ip, [_vp, _ip, _vp, _ip, ctypes.POINTER(ctypes.c_longlong)]),
+    "glsfft_server_wait": (_ip, [_vp, ctypes.c_longlong, _dp, _dp, ctypes.c_double]),
+    "glsfft_server_replay": (_ip, [_vp, _ip, _dp, ctypes.POINTER(_ip), ctypes.POINTER(_vp), _ip,
+                                   _dp, _dp]),
+    "glsfft_server_stats": (_ip, [_vp, ctypes.POINTER(ctypes.c_longlong)]),
+    "glsfft_server_destroy": (_ip, [_vp]),
 }
 
 _lib = None
@@ -212,6 +220,73 @@ class Batch:
     def close(self) -> None:
         if self.handle:
             lib().glsfft_batch_destroy(self.handle)
+            self.handle = _vp()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Server:
+    """phaseCorrelate serving loop (glsfft_server): resident reference
+    spectra, HBM-budget admission, continuous batching over `slots` streams."""
+
+    STATS = ("admitted", "completed", "failed", "peak_in_flight", "peak_queue",
+             "budget_bytes", "peak_budget_bytes", "references")
+
+    def __init__(self, ctx: Context, slots: int = 8, hbm_budget: int = 4 << 30):
+        self.handle = _vp()
+        check(lib().glsfft_server_create(ctx.handle, int(slots), int(hbm_budget),
+                                         ctypes.byref(self.handle)), "glsfft_server_create")
+
+    def add_reference(self, frame: int, window: int | None, rows: int, cols: int) -> int:
+        rid = _ip()
+        check(lib().glsfft_server_add_reference(self.handle, frame, window or None, rows, cols,
+                                                ctypes.byref(rid)), "server_add_reference")
+        return rid.value
+
+    def submit(self, ref_id: int, host_frame: int, box: int = 5) -> int:
+        t = ctypes.c_longlong()
+        check(lib().glsfft_server_submit(self.handle, int(ref_id), host_frame, int(box),
+                                         ctypes.byref(t)), "server_submit")
+        return t.value
+
+    def wait(self, ticket: int, timeout_s: float = 30.0):
+        res = (ctypes.c_double * 5)()
+        lat = ctypes.c_double()
+        check(lib().glsfft_server_wait(self.handle, ctypes.c_longlong(ticket),
+                                       ctypes.cast(res, _dp), ctypes.byref(lat),
+                                       float(timeout_s)), "server_wait")
+        return list(res), lat.value
+
+    def replay(self, offsets_s, ref_ids, host_frames, box: int = 5):
+        n = len(offsets_s)
+        offs = (ctypes.c_double * n)(*[float(x) for x in offsets_s])
+        refs = (_ip * n)(*[int(x) for x in ref_ids])
+        frames = (_vp * n)(*[int(x) for x in host_frames])
+        lat = (ctypes.c_double * n)()
+        res = (ctypes.c_double * (5 * n))()
+        check(lib().glsfft_server_replay(self.handle, n, ctypes.cast(offs, _dp), refs, frames,
+                                         int(box), ctypes.cast(lat, _dp), ctypes.cast(res, _dp)),
+              "server_replay")
+        return list(lat), [list(res[5 * k:5 * k + 5]) for k in range(n)]
+
+    def stats(self) -> dict:
+        out = (ctypes.c_longlong * 8)()
+        check(lib().glsfft_server_stats(self.handle, out), "server_stats")
+        return dict(zip(self.STATS, list(out)))
+
+    def close(self) -> None:
+        if self.handle:
+            lib().glsfft_server_destroy(self.handle)
             self.handle = _vp()
 
     def __enter__(self):

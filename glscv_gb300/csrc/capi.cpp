@@ -66,15 +66,15 @@ namespace {
 
 inline bool is_pow2(int x) { return x > 0 && (x & (x - 1)) == 0; }
 
-int check_dims(int rows, int cols) {
+inline bool aligned(const void *p, size_t a) { return (reinterpret_cast<uintptr_t>(p) % a) == 0; }
+
+}  // namespace
+
+int glsfft::check_dims(int rows, int cols) {
     if (rows < 1 || cols < 1 || rows > kMaxLen || cols > kMaxLen) return GLSFFT_ERROR_SIZE;
     if (!is_pow2(rows) || !is_pow2(cols)) return GLSFFT_ERROR_NOT_POW2;
     return GLSFFT_SUCCESS;
 }
-
-inline bool aligned(const void *p, size_t a) { return (reinterpret_cast<uintptr_t>(p) % a) == 0; }
-
-}  // namespace
 
 int glsfft::cuda_status(cudaError_t e) {
     if (e == cudaSuccess) return GLSFFT_SUCCESS;

@@ -32,6 +32,7 @@ class DeviceGuard {
 };
 
 int cuda_status(cudaError_t e);
+int check_dims(int rows, int cols);  // 1..kMaxLen, powers of two
 int ensure_workspace(glsfft_context ctx, size_t bytes);
 int check_fft_args(const void *src, const void *dst, int rows, int cols, int flags, bool real_in);
 int check_poc_args(glsfft_context ctx, const float *src1, const float *src2,

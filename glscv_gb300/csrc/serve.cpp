@@ -1,0 +1,494 @@
+// serve.cpp -- phaseCorrelate serving loop with resident reference spectra
+// and continuous batching.
+//
+// A server owns one device arena (its whole HBM budget, reserved once), a set
+// of slots (a CUDA stream, an event and a pinned result buffer each), and two
+// native threads:
+//   * the dispatcher admits queued requests in arrival order as soon as a slot
+//     is free and the request's workspace fits in the arena (looking a few
+//     requests past a head that does not fit yet), and launches the request's
+//     whole pipeline on the slot's stream: host->device copy of the frame,
+//     windowed row FFT, phase-only column kernel against the resident
+//     reference spectrum (so 2 FFTs per request instead of 3), inverse row FFT
+//     with the argmax, FP64 centroid, device->host copy of the result;
+//   * the completion poller watches the slots' events, stamps completion
+//     times, returns workspaces to the arena and wakes the dispatcher.
+// Requests that arrive while others run are admitted as resources free up,
+// so their kernels overlap on the device.  The kernels are deterministic, so
+// a request's result does not depend on what runs beside it.
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <mutex>
+#include <new>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "arena.h"
+#include "capi_internal.h"
+#include "glsfft_internal.h"
+
+using namespace glsfft;
+using Clock = std::chrono::steady_clock;
+
+namespace {
+
+struct Reference {
+    int rows = 0, cols = 0;
+    size_t spec_off = 0, win_off = 0;
+    bool has_window = false;
+};
+
+enum { REQ_QUEUED = 0, REQ_RUNNING = 1, REQ_DONE = 2, REQ_FAILED = 3 };
+
+struct Request {
+    int ref = 0;
+    const float *frame = nullptr;  // host pointer, valid until completion
+    int box = 5;
+    Clock::time_point arrival, done_at;
+    int state = REQ_QUEUED;
+    int status = GLSFFT_SUCCESS;
+    int slot = -1;
+    size_t ws_off = Arena::kFail;
+    double result[5] = {0, 0, 0, 0, 0};
+};
+
+struct Slot {
+    cudaStream_t stream = nullptr;
+    cudaEvent_t done = nullptr;
+    double *h_result = nullptr;  // pinned, 8 doubles
+    long long ticket = -1;
+    bool launched = false;  // the event of this ticket's pipeline is recorded
+};
+
+size_t workspace_bytes(int rows, int cols) {
+    const size_t n = (size_t)rows * cols;
+    // frame (float) | row-pass / column output (complex) | surface (float) | key | result
+    return Arena::round_up(4 * n) + Arena::round_up(8 * n) + Arena::round_up(4 * n) + 256;
+}
+
+}  // namespace
+
+struct glsfft_server_s {
+    glsfft_context ctx = nullptr;
+    int device = 0;
+    char *d_base = nullptr;
+    Arena arena;
+    std::vector<Reference> refs;
+    std::vector<Slot> slots;
+    std::mutex mu;
+    std::condition_variable cv_dispatch, cv_poll, cv_done;
+    std::deque<long long> queue;
+    std::unordered_map<long long, Request> reqs;
+    long long next_ticket = 1;
+    int in_flight = 0;
+    bool stop = false;
+    std::thread dispatcher, poller;
+    // counters
+    long long admitted = 0, completed = 0, failed = 0;
+    long long peak_in_flight = 0, peak_queue = 0;
+    size_t peak_arena = 0;
+};
+
+namespace {
+
+// Launch one request's pipeline on its slot.  Called without the lock held.
+int launch_request(glsfft_server srv, const Reference &ref, const Request &rq, Slot &slot) {
+    const int rows = ref.rows, cols = ref.cols;
+    const size_t n = (size_t)rows * cols;
+    char *ws = srv->d_base + rq.ws_off;
+    float *frame = reinterpret_cast<float *>(ws);
+    float2 *f2 = reinterpret_cast<float2 *>(ws + Arena::round_up(4 * n));
+    float *surface = reinterpret_cast<float *>(ws + Arena::round_up(4 * n) + Arena::round_up(8 * n));
+    char *tail = ws + Arena::round_up(4 * n) + Arena::round_up(8 * n) + Arena::round_up(4 * n);
+    auto *key = reinterpret_cast<unsigned long long *>(tail);
+    auto *res = reinterpret_cast<double *>(tail + 64);
+    const float2 *spec = reinterpret_cast<const float2 *>(srv->d_base + ref.spec_off);
+    const float *win = ref.has_window ? reinterpret_cast<const float *>(srv->d_base + ref.win_off) : nullptr;
+    cudaStream_t s = slot.stream;
+
+    cudaError_t e = cudaMemcpyAsync(frame, rq.frame, 4 * n, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(key, 0, sizeof(unsigned long long), s);
+    if (e != cudaSuccess) return cuda_status(e);
+    PassArgs a{};
+    a.in0 = frame;
+    a.out0 = f2;
+    a.window = win;
+    a.rows = rows;
+    a.cols = cols;
+    a.scale = 1.0f;
+    a.tw = srv->ctx->d_tw;
+    e = launch_rows(cols, win ? LD_R1W : LD_R1, ST_C2, a, 1, s);
+    if (e != cudaSuccess) return cuda_status(e);
+    PassArgs b{};
+    b.in0 = spec;  // resident reference spectrum (already column-transformed)
+    b.in1 = f2;
+    b.out0 = f2;   // in place over the frame's row-pass output
+    b.rows = rows;
+    b.cols = cols;
+    b.scale = 1.0f;
+    b.flags = PF_F1_SPECTRUM;
+    b.tw = srv->ctx->d_tw;
+    e = launch_poc_cols(rows, b, s);
+    if (e != cudaSuccess) return cuda_status(e);
+    PassArgs c{};
+    c.in0 = f2;
+    c.out0 = surface;
+    c.rows = rows;
+    c.cols = cols;
+    c.scale = 1.0f;
+    c.flags = PF_SHIFT_ROWS | PF_SHIFT_COLS;
+    c.key = key;
+    c.tw = srv->ctx->d_tw;
+    e = launch_rows(cols, LD_C2, ST_RE_ARGMAX, c, 1, s);
+    if (e == cudaSuccess) e = launch_poc_finish(surface, rows, cols, rq.box, key, res, s);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(slot.h_result, res, 5 * sizeof(double), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaEventRecord(slot.done, s);
+    return cuda_status(e);
+}
+
+void dispatcher_main(glsfft_server srv) {
+    cudaSetDevice(srv->device);
+    std::unique_lock<std::mutex> lock(srv->mu);
+    constexpr size_t kLookahead = 8;
+    while (!srv->stop) {
+        bool progress = false;
+        for (size_t qi = 0; qi < srv->queue.size() && qi < kLookahead;) {
+            const long long ticket = srv->queue[qi];
+            Request &rq = srv->reqs[ticket];
+            const Reference ref = srv->refs[rq.ref];
+            const size_t need = workspace_bytes(ref.rows, ref.cols);
+            int free_slot = -1;
+            for (int i = 0; i < (int)srv->slots.size(); i++)
+                if (srv->slots[i].ticket < 0) {
+                    free_slot = i;
+                    break;
+                }
+            if (free_slot < 0) break;  // every slot busy: nothing more to admit now
+            const size_t off = srv->arena.alloc(need);
+            if (off == Arena::kFail) {
+                qi++;  // look past a request that does not fit yet
+                continue;
+            }
+            srv->queue.erase(srv->queue.begin() + qi);
+            rq.ws_off = off;
+            rq.slot = free_slot;
+            rq.state = REQ_RUNNING;
+            Slot &slot = srv->slots[free_slot];
+            slot.ticket = ticket;
+            slot.launched = false;  // not pollable until its event is recorded
+            srv->in_flight++;
+            srv->admitted++;
+            srv->peak_in_flight = std::max<long long>(srv->peak_in_flight, srv->in_flight);
+            srv->peak_arena = std::max(srv->peak_arena, srv->arena.in_use());
+            const Request snapshot = rq;
+            lock.unlock();
+            const int st = launch_request(srv, ref, snapshot, slot);
+            lock.lock();
+            if (st != GLSFFT_SUCCESS) {
+                Request &r2 = srv->reqs[ticket];
+                r2.state = REQ_FAILED;
+                r2.status = st;
+                r2.done_at = Clock::now();
+                srv->arena.release(r2.ws_off);
+                srv->slots[free_slot].ticket = -1;
+                srv->in_flight--;
+                srv->failed++;
+                srv->cv_done.notify_all();
+            } else {
+                srv->slots[free_slot].launched = true;
+            }
+            srv->cv_poll.notify_one();
+            progress = true;
+        }
+        if (!progress) srv->cv_dispatch.wait(lock);
+    }
+}
+
+void poller_main(glsfft_server srv) {
+    cudaSetDevice(srv->device);
+    std::unique_lock<std::mutex> lock(srv->mu);
+    for (;;) {
+        if (srv->in_flight == 0) {
+            if (srv->stop) break;
+            srv->cv_poll.wait(lock);
+            continue;
+        }
+        bool any = false;
+        for (int i = 0; i < (int)srv->slots.size(); i++) {
+            Slot &slot = srv->slots[i];
+            if (slot.ticket < 0 || !slot.launched) continue;
+            const cudaError_t q = cudaEventQuery(slot.done);
+            if (q == cudaErrorNotReady) continue;
+            Request &rq = srv->reqs[slot.ticket];
+            rq.done_at = Clock::now();
+            if (q == cudaSuccess) {
+                std::memcpy(rq.result, slot.h_result, sizeof(rq.result));
+                rq.state = REQ_DONE;
+                srv->completed++;
+            } else {
+                cudaGetLastError();
+                rq.state = REQ_FAILED;
+                rq.status = GLSFFT_ERROR_CUDA;
+                srv->failed++;
+            }
+            srv->arena.release(rq.ws_off);
+            slot.ticket = -1;
+            srv->in_flight--;
+            any = true;
+        }
+        if (any) {
+            srv->cv_dispatch.notify_one();
+            srv->cv_done.notify_all();
+        } else {
+            // requests are in flight: keep polling (a timed sleep would add
+            // the kernel's timer slack, tens of microseconds, to every latency)
+            lock.unlock();
+            std::this_thread::yield();
+            lock.lock();
+        }
+    }
+}
+
+long long submit_locked(glsfft_server srv, int ref_id, const float *frame, int box,
+                        Clock::time_point arrival) {
+    const long long ticket = srv->next_ticket++;
+    Request rq;
+    rq.ref = ref_id;
+    rq.frame = frame;
+    rq.box = box;
+    rq.arrival = arrival;
+    srv->reqs.emplace(ticket, rq);
+    srv->queue.push_back(ticket);
+    srv->peak_queue = std::max<long long>(srv->peak_queue, (long long)srv->queue.size());
+    return ticket;
+}
+
+}  // namespace
+
+extern "C" {
+
+int glsfft_server_create(glsfft_context ctx, int slots, size_t hbm_budget, glsfft_server *out) {
+    if (!out) return GLSFFT_ERROR_INVALID_VALUE;
+    *out = nullptr;
+    if (!ctx || slots < 1 || slots > 64 || hbm_budget < Arena::kAlign) return GLSFFT_ERROR_INVALID_VALUE;
+    DeviceGuard g(ctx->device);
+    if (!g.ok()) return GLSFFT_ERROR_CUDA;
+    auto *srv = new (std::nothrow) glsfft_server_s();
+    if (!srv) return GLSFFT_ERROR_OUT_OF_MEMORY;
+    srv->ctx = ctx;
+    srv->device = ctx->device;
+    if (cudaMalloc(&srv->d_base, hbm_budget) != cudaSuccess) {
+        cudaGetLastError();
+        delete srv;
+        return GLSFFT_ERROR_OUT_OF_MEMORY;
+    }
+    srv->arena.reset(hbm_budget);
+    srv->slots.resize(slots);
+    for (auto &s : srv->slots) {
+        cudaError_t e = cudaStreamCreateWithFlags(&s.stream, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s.done, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaMallocHost(&s.h_result, 8 * sizeof(double));
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            for (auto &t : srv->slots) {
+                if (t.stream) cudaStreamDestroy(t.stream);
+                if (t.done) cudaEventDestroy(t.done);
+                if (t.h_result) cudaFreeHost(t.h_result);
+            }
+            cudaFree(srv->d_base);
+            delete srv;
+            return GLSFFT_ERROR_CUDA;
+        }
+    }
+    srv->dispatcher = std::thread(dispatcher_main, srv);
+    srv->poller = std::thread(poller_main, srv);
+    *out = srv;
+    return GLSFFT_SUCCESS;
+}
+
+int glsfft_server_add_reference(glsfft_server srv, const float *frame, const float *window,
+                                int rows, int cols, int *ref_id) {
+    if (!srv || !frame || !ref_id) return GLSFFT_ERROR_INVALID_VALUE;
+    int st = check_dims(rows, cols);
+    if (st) return st;
+    if ((reinterpret_cast<uintptr_t>(frame) & 3) || (window && (reinterpret_cast<uintptr_t>(window) & 3)))
+        return GLSFFT_ERROR_MISALIGNED;
+    DeviceGuard g(srv->device);
+    if (!g.ok()) return GLSFFT_ERROR_CUDA;
+    const size_t n = (size_t)rows * cols;
+    Reference ref;
+    ref.rows = rows;
+    ref.cols = cols;
+    ref.has_window = window != nullptr;
+    {
+        std::lock_guard<std::mutex> lock(srv->mu);
+        ref.spec_off = srv->arena.alloc(8 * n);
+        if (ref.spec_off == Arena::kFail) return GLSFFT_ERROR_BUDGET;
+        if (window) {
+            ref.win_off = srv->arena.alloc(4 * n);
+            if (ref.win_off == Arena::kFail) {
+                srv->arena.release(ref.spec_off);
+                return GLSFFT_ERROR_BUDGET;
+            }
+        }
+        srv->peak_arena = std::max(srv->peak_arena, srv->arena.in_use());
+    }
+    float2 *spec = reinterpret_cast<float2 *>(srv->d_base + ref.spec_off);
+    float *win = window ? reinterpret_cast<float *>(srv->d_base + ref.win_off) : nullptr;
+    cudaStream_t s = srv->slots[0].stream;
+    cudaError_t e = cudaSuccess;
+    if (window) e = cudaMemcpyAsync(win, window, 4 * n, cudaMemcpyDeviceToDevice, s);
+    if (e != cudaSuccess) return cuda_status(e);
+    // the reference's forward spectrum of window x frame: rows pass with the
+    // window fused into the load, then the columns pass in place
+    PassArgs a{};
+    a.in0 = frame;
+    a.out0 = spec;
+    a.window = win;
+    a.rows = rows;
+    a.cols = cols;
+    a.scale = 1.0f;
+    a.tw = srv->ctx->d_tw;
+    e = launch_rows(cols, win ? LD_R1W : LD_R1, ST_C2, a, 1, s);
+    if (e == cudaSuccess && rows > 1) {
+        PassArgs b{};
+        b.in0 = spec;
+        b.out0 = spec;
+        b.rows = rows;
+        b.cols = cols;
+        b.scale = 1.0f;
+        b.tw = srv->ctx->d_tw;
+        e = launch_cols(rows, LD_C2, ST_C2, b, 1, s);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cuda_status(e);
+    std::lock_guard<std::mutex> lock(srv->mu);
+    srv->refs.push_back(ref);
+    *ref_id = (int)srv->refs.size() - 1;
+    return GLSFFT_SUCCESS;
+}
+
+int glsfft_server_submit(glsfft_server srv, int ref_id, const float *host_frame, int box,
+                         long long *ticket) {
+    if (!srv || !host_frame || !ticket || box < 1) return GLSFFT_ERROR_INVALID_VALUE;
+    std::lock_guard<std::mutex> lock(srv->mu);
+    if (ref_id < 0 || ref_id >= (int)srv->refs.size()) return GLSFFT_ERROR_INVALID_VALUE;
+    const Reference &ref = srv->refs[ref_id];
+    if (workspace_bytes(ref.rows, ref.cols) > srv->arena.capacity()) return GLSFFT_ERROR_BUDGET;
+    *ticket = submit_locked(srv, ref_id, host_frame, box, Clock::now());
+    srv->cv_dispatch.notify_one();
+    return GLSFFT_SUCCESS;
+}
+
+int glsfft_server_wait(glsfft_server srv, long long ticket, double *result5, double *latency_s,
+                       double timeout_s) {
+    if (!srv) return GLSFFT_ERROR_INVALID_VALUE;
+    std::unique_lock<std::mutex> lock(srv->mu);
+    auto it = srv->reqs.find(ticket);
+    if (it == srv->reqs.end()) return GLSFFT_ERROR_INVALID_VALUE;
+    const auto deadline = Clock::now() + std::chrono::duration_cast<Clock::duration>(
+                                             std::chrono::duration<double>(timeout_s));
+    while (it->second.state < REQ_DONE) {
+        if (srv->cv_done.wait_until(lock, deadline) == std::cv_status::timeout &&
+            it->second.state < REQ_DONE)
+            return GLSFFT_ERROR_TIMEOUT;
+        it = srv->reqs.find(ticket);
+    }
+    const Request rq = it->second;
+    srv->reqs.erase(it);
+    if (result5) std::memcpy(result5, rq.result, sizeof(rq.result));
+    if (latency_s) *latency_s = std::chrono::duration<double>(rq.done_at - rq.arrival).count();
+    return rq.state == REQ_DONE ? GLSFFT_SUCCESS : rq.status;
+}
+
+int glsfft_server_replay(glsfft_server srv, int n, const double *offsets_s, const int *ref_ids,
+                         const float *const *host_frames, int box, double *latencies_s,
+                         double *results5) {
+    if (!srv || n < 1 || !offsets_s || !ref_ids || !host_frames || !latencies_s || box < 1)
+        return GLSFFT_ERROR_INVALID_VALUE;
+    {
+        std::lock_guard<std::mutex> lock(srv->mu);
+        for (int k = 0; k < n; k++) {
+            if (ref_ids[k] < 0 || ref_ids[k] >= (int)srv->refs.size() || !host_frames[k])
+                return GLSFFT_ERROR_INVALID_VALUE;
+            const Reference &ref = srv->refs[ref_ids[k]];
+            if (workspace_bytes(ref.rows, ref.cols) > srv->arena.capacity()) return GLSFFT_ERROR_BUDGET;
+        }
+    }
+    std::vector<long long> tickets(n);
+    const Clock::time_point t0 = Clock::now();
+    for (int k = 0; k < n; k++) {
+        // open-loop arrivals: latency counts from the scheduled arrival time
+        const Clock::time_point at =
+            t0 + std::chrono::duration_cast<Clock::duration>(std::chrono::duration<double>(offsets_s[k]));
+        while (Clock::now() < at) {
+            const auto left = at - Clock::now();
+            if (left > std::chrono::microseconds(200)) std::this_thread::sleep_for(left / 2);
+        }
+        std::lock_guard<std::mutex> lock(srv->mu);
+        tickets[k] = submit_locked(srv, ref_ids[k], host_frames[k], box, at);
+        srv->cv_dispatch.notify_one();
+    }
+    int status = GLSFFT_SUCCESS;
+    for (int k = 0; k < n; k++) {
+        double r[5];
+        const int st = glsfft_server_wait(srv, tickets[k], r, &latencies_s[k], 60.0);
+        if (st && !status) status = st;
+        if (results5) std::memcpy(results5 + 5 * (size_t)k, r, sizeof(r));
+    }
+    return status;
+}
+
+int glsfft_server_stats(glsfft_server srv, long long *out8) {
+    if (!srv || !out8) return GLSFFT_ERROR_INVALID_VALUE;
+    std::lock_guard<std::mutex> lock(srv->mu);
+    out8[0] = srv->admitted;
+    out8[1] = srv->completed;
+    out8[2] = srv->failed;
+    out8[3] = srv->peak_in_flight;
+    out8[4] = srv->peak_queue;
+    out8[5] = (long long)srv->arena.capacity();
+    out8[6] = (long long)srv->peak_arena;
+    out8[7] = (long long)srv->refs.size();
+    return GLSFFT_SUCCESS;
+}
+
+int glsfft_server_destroy(glsfft_server srv) {
+    if (!srv) return GLSFFT_ERROR_INVALID_VALUE;
+    {
+        std::lock_guard<std::mutex> lock(srv->mu);
+        srv->stop = true;
+        // requests still queued are dropped; running ones finish below
+        for (long long t : srv->queue) {
+            auto &rq = srv->reqs[t];
+            rq.state = REQ_FAILED;
+            rq.status = GLSFFT_ERROR_INVALID_VALUE;
+        }
+        srv->queue.clear();
+    }
+    srv->cv_dispatch.notify_all();
+    srv->cv_poll.notify_all();
+    srv->cv_done.notify_all();
+    if (srv->dispatcher.joinable()) srv->dispatcher.join();
+    if (srv->poller.joinable()) srv->poller.join();
+    DeviceGuard g(srv->device);
+    for (auto &s : srv->slots) {
+        if (s.stream) {
+            cudaStreamSynchronize(s.stream);
+            cudaStreamDestroy(s.stream);
+        }
+        if (s.done) cudaEventDestroy(s.done);
+        if (s.h_result) cudaFreeHost(s.h_result);
+    }
+    if (srv->d_base) cudaFree(srv->d_base);
+    delete srv;
+    return GLSFFT_SUCCESS;
+}
+
+}  // extern "C"

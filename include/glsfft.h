@@ -215,6 +215,67 @@ GLSFFT_API int glsfft_phase_correlate_async(glsfft_context ctx, const float *src
 GLSFFT_API int glsfft_phase_correlate_surface(glsfft_context ctx, float *dst, size_t count,
                                               void *stream);
 
+/*
+ * phaseCorrelate serving loop (no reference counterpart: glsCam calls
+ * gls::phaseCorrelate one frame at a time, glsCam/glsCam.cpp).  A server
+ * reserves `hbm_budget` bytes of device memory once and carves resident
+ * reference spectra and per-request workspaces (16 * rows * cols bytes + 256)
+ * out of it; `slots` streams let up to that many requests run at once.  A
+ * native dispatcher admits queued requests in arrival order as a slot frees
+ * and their workspace fits (continuous batching; it may admit a request
+ * behind one that does not fit yet), and a native poller completes them.
+ * Each request computes phaseCorrelate(reference frame, request frame) with
+ * the reference's window, using the resident reference spectrum, so only
+ * two FFTs run per request.
+ */
+typedef struct glsfft_server_s *glsfft_server;
+
+GLSFFT_API int glsfft_server_create(glsfft_context ctx, int slots, size_t hbm_budget,
+                                    glsfft_server *server);
+
+/*
+ * Make a reference resident: its spectrum FFT2(window x frame) is computed
+ * once (frame, window: CV_32FC1 device images; window may be NULL) and
+ * kept in the server's budget.  Synchronous.  Returns its id in *ref_id.
+ */
+GLSFFT_API int glsfft_server_add_reference(glsfft_server server, const float *frame,
+                                           const float *window, int rows, int cols, int *ref_id);
+
+/*
+ * Queue a request: the shift of host_frame (CV_32FC1, the reference's size,
+ * host memory that stays valid until the request completes; page-locked
+ * memory keeps the copy asynchronous) relative to reference ref_id.
+ * Returns at once with a ticket.  GLSFFT_ERROR_BUDGET when the request could
+ * never fit in the budget.
+ */
+GLSFFT_API int glsfft_server_submit(glsfft_server server, int ref_id, const float *host_frame,
+                                    int box, long long *ticket);
+
+/*
+ * Wait (at most timeout_s) for a request; fills {dx, dy, response, peak
+ * index, peak value} and the latency from arrival to completion, then forgets
+ * the ticket.  GLSFFT_ERROR_TIMEOUT when it is still running.
+ */
+GLSFFT_API int glsfft_server_wait(glsfft_server server, long long ticket, double *result5,
+                                  double *latency_s, double timeout_s);
+
+/*
+ * Open-loop load: request k arrives offsets_s[k] seconds after the call
+ * (submitted by the calling thread on schedule), for reference ref_ids[k]
+ * and frame host_frames[k]; blocks until all complete and writes each
+ * latency (from its scheduled arrival) and result (5 doubles, may be NULL).
+ */
+GLSFFT_API int glsfft_server_replay(glsfft_server server, int n, const double *offsets_s,
+                                    const int *ref_ids, const float *const *host_frames, int box,
+                                    double *latencies_s, double *results5);
+
+/* Counters: admitted, completed, failed, peak in flight, peak queue length,
+ * budget bytes, peak budget bytes in use, resident references. */
+GLSFFT_API int glsfft_server_stats(glsfft_server server, long long *out8);
+
+/* Drop queued requests, finish running ones, free everything. */
+GLSFFT_API int glsfft_server_destroy(glsfft_server server);
+
 /* Largest image (rows * cols) glsfft_phase_correlate_noalloc accepts. */
 #define GLSFFT_NOALLOC_MAX_PIXELS (512 * 512)
 

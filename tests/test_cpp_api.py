@@ -38,3 +38,15 @@ def test_cpp_api_runs(cpp_binary, torch_cuda):
     res = subprocess.run([str(cpp_binary)], capture_output=True, text=True, timeout=300)
     assert res.returncode == 0, res.stdout + res.stderr
     assert "ALL OK" in res.stdout
+
+
+def test_arena_allocator_host_unit(tmp_path):
+    """The serving loop's device-memory arena, compiled without CUDA."""
+    src = ROOT / "tests" / "cpp" / "test_arena.cpp"
+    out = tmp_path / "test_arena"
+    res = subprocess.run(["g++", "-std=c++17", "-O1", "-Wall",
+                          f"-I{ROOT / 'glscv_gb300' / 'csrc'}", str(src), "-o", str(out)],
+                         capture_output=True, text=True)
+    assert res.returncode == 0, res.stderr
+    run = subprocess.run([str(out)], capture_output=True, text=True, timeout=60)
+    assert run.returncode == 0 and "ALL OK" in run.stdout, run.stdout

@@ -1,0 +1,123 @@
+"""phaseCorrelate serving loop (glsfft_server) on the GPU.
+
+* Each request's result is the same alone and in a mix of overlapping
+  requests of other sizes (bit for bit: the kernels are deterministic), and
+  the same as the context-based gls::phaseCorrelate on the same frames.
+* Admission by HBM budget: with room for one workspace at a time every
+  request still completes, one at a time; a request that can never fit is
+  refused at submit.
+* Poisson replay completes every request with the right shift.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import glscv_gb300 as g
+from glscv_gb300 import workloads as wl
+from tests.gpu_util import gpu_phase_correlate
+
+pytestmark = pytest.mark.gpu
+
+
+def _pinned(torch, arr):
+    t = torch.empty(arr.shape, dtype=torch.float32, pin_memory=True)
+    t.copy_(torch.from_numpy(np.ascontiguousarray(arr, np.float32)))
+    return t
+
+
+def _setup(torch, srv, sizes, seed=0):
+    """One reference per size (a uniform random image, the reference test's
+    input, UnitTest_glsPhaseCorrelate.cpp:87, + Hann window) and, for each, a
+    few circularly shifted noisy frames in page-locked host memory."""
+    refs, frames = [], []
+    keep = []
+    for i, n in enumerate(sizes):
+        a = np.random.default_rng(seed + i).uniform(0, 1, (n, n)).astype(np.float32)
+        w = wl.hann_window(n, n)
+        da, dw = torch.from_numpy(a).cuda(), torch.from_numpy(w).cuda()
+        rid = srv.add_reference(da.data_ptr(), dw.data_ptr(), n, n)
+        keep += [da, dw]
+        for k in range(3):
+            rng = np.random.default_rng(100 * i + k)
+            dx, dy = int(rng.integers(-n // 8, n // 8)), int(rng.integers(-n // 8, n // 8))
+            b = np.roll(a, (dy, dx), axis=(0, 1)) + rng.normal(0, 0.01, a.shape)
+            hb = _pinned(torch, b)
+            frames.append((rid, hb, (dx, dy), a, b.astype(np.float32), w))
+        refs.append(rid)
+    return refs, frames, keep
+
+
+def test_alone_equals_mix_equals_context_path(ctx, torch_cuda):
+    torch = torch_cuda
+    with g.Server(ctx, slots=8, hbm_budget=1 << 30) as srv:
+        refs, frames, keep = _setup(torch, srv, [256, 512, 1024])
+        alone = []
+        for rid, hb, _, _, _, _ in frames:
+            t = srv.submit(rid, hb.data_ptr())
+            alone.append(srv.wait(t)[0])
+        order = list(range(len(frames))) * 3
+        np.random.default_rng(1).shuffle(order)
+        tickets = [(i, srv.submit(frames[i][0], frames[i][1].data_ptr())) for i in order]
+        mix = [(i, srv.wait(t)[0]) for i, t in tickets]
+        st = srv.stats()
+        assert st["peak_in_flight"] > 1, st  # requests really overlapped
+        for i, r in mix:
+            assert r == alone[i], (i, r, alone[i])
+        for i, (rid, hb, (dx, dy), a, b, w) in enumerate(frames):
+            (gx, gy), resp, _ = gpu_phase_correlate(ctx, torch, a, b, w)
+            assert abs(alone[i][0] - gx) < 1e-9 and abs(alone[i][1] - gy) < 1e-9
+            assert abs(alone[i][2] - resp) < 1e-9
+            assert abs(alone[i][0] - dx) < 0.25 and abs(alone[i][1] - dy) < 0.25
+
+
+def test_budget_admission_serialises_and_refuses(ctx, torch_cuda):
+    torch = torch_cuda
+    n = 512
+    ref_bytes = 8 * n * n + 4 * n * n           # spectrum + window copy
+    ws_bytes = 16 * n * n + 256 + 3 * 256       # one request's workspace (rounded)
+    with g.Server(ctx, slots=4, hbm_budget=ref_bytes + ws_bytes + 4096) as srv:
+        refs, frames, keep = _setup(torch, srv, [n])
+        tickets = [srv.submit(rid, hb.data_ptr()) for rid, hb, *_ in frames * 4]
+        outs = [srv.wait(t)[0] for t in tickets]
+        st = srv.stats()
+        assert st["completed"] == len(tickets) and st["failed"] == 0
+        assert st["peak_in_flight"] == 1, st
+        for k, (rid, hb, (dx, dy), *_rest) in enumerate(frames * 4):
+            assert abs(outs[k][0] - dx) < 0.25 and abs(outs[k][1] - dy) < 0.25
+    with g.Server(ctx, slots=2, hbm_budget=16 * 64 * 64 * 4) as small:
+        d = torch.zeros((64, 64), dtype=torch.float32, device="cuda")
+        rid = small.add_reference(d.data_ptr(), None, 64, 64)
+        big = torch.zeros((64, 64), dtype=torch.float32, pin_memory=True)
+        with pytest.raises(g.GlsError) as e:
+            small.add_reference(d.data_ptr(), None, 1024, 1024)  # spectrum does not fit
+        assert e.value.status == 7
+        small.wait(small.submit(rid, big.data_ptr()))
+
+
+def test_poisson_replay(ctx, torch_cuda):
+    torch = torch_cuda
+    with g.Server(ctx, slots=8, hbm_budget=1 << 30) as srv:
+        refs, frames, keep = _setup(torch, srv, [256, 512, 1024])
+        rng = np.random.default_rng(5)
+        n = 200
+        offsets = np.cumsum(rng.exponential(1 / 2000.0, n))
+        pick = rng.integers(0, len(frames), n)
+        lat, res = srv.replay(offsets, [frames[i][0] for i in pick],
+                              [frames[i][1].data_ptr() for i in pick])
+        assert srv.stats()["completed"] >= n
+        for k, i in enumerate(pick):
+            dx, dy = frames[i][2]
+            assert abs(res[k][0] - dx) < 0.25 and abs(res[k][1] - dy) < 0.25
+        assert min(lat) > 0 and np.percentile(lat, 99) < 0.05
+
+
+def test_submit_errors_and_destroy_with_queue(ctx, torch_cuda):
+    torch = torch_cuda
+    srv = g.Server(ctx, slots=2, hbm_budget=256 << 20)
+    refs, frames, keep = _setup(torch, srv, [256])
+    with pytest.raises(g.GlsError):
+        srv.submit(99, frames[0][1].data_ptr())
+    for _ in range(50):
+        srv.submit(frames[0][0], frames[0][1].data_ptr())
+    srv.close()  # drops the queue, finishes the running requests, returns
