@@ -269,6 +269,54 @@ def serving_sweep(g, ctx, torch, seconds: float = 0.5, max_requests: int = 4000)
     return out
 
 
+# ---------------------------------------------------------- precision form
+def precision_form(ctx, torch, s) -> dict:
+    """Split-FP16 tensor-core FFT vs the FP32 CUDA-core path: time (forward,
+    CUDA events) and error vs FP64 on 4096^2 and on a batch of 64 x 1024^2,
+    uniform[-1,1] and 1e3 dynamic-range inputs (seed 4)."""
+    import numpy as np
+    from glscv_gb300 import workloads as wl
+
+    def timed(fn, k=5):
+        fn()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(k):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / k
+
+    out = []
+    for count, n in ((1, 4096), (64, 1024)):
+        row = {"shape": f"{count}x{n}x{n}", "forward_ms": {}, "gflops": {}, "rel_l2": {},
+               "max_abs": {}}
+        for kind, gen in (("uniform", wl.complex_uniform), ("dynamic_range", wl.complex_dynamic_range)):
+            x = gen(n, n, 4)
+            d = torch.from_numpy(np.stack([x] * count)).cuda()
+            o = torch.empty_like(d)
+            ref = np.fft.fft2(x.astype(np.complex128))
+            for form in ("fp32", "tc"):
+                fn = (lambda: ctx.fft2d_batched(d.data_ptr(), o.data_ptr(), count, n, n, 0, s)) \
+                    if form == "fp32" else \
+                    (lambda: ctx.fft2d_tc(d.data_ptr(), o.data_ptr(), count, n, n, 0, s))
+                ms = timed(fn)
+                y = o[0].cpu().numpy().astype(np.complex128)
+                row["rel_l2"][f"{form}_{kind}"] = float(np.linalg.norm(y - ref) / np.linalg.norm(ref))
+                row["max_abs"][f"{form}_{kind}"] = float(np.max(np.abs(y - ref)))
+                if kind == "uniform":
+                    row["forward_ms"][form] = round(ms, 4)
+                    row["gflops"][form] = round(count * 5 * n * n * math.log2(n * n) / (ms * 1e-3) / 1e9, 1)
+            del d, o
+        row["tc_over_fp32_time"] = round(row["forward_ms"]["tc"] / row["forward_ms"]["fp32"], 3)
+        out.append(row)
+    return {"form": "four-step, DFT stages as mma.sync m16n8k16 f16 products with hi/lo split "
+                    "(3 products, FP32 accumulate, separate correction accumulator)",
+            "kept_as_default": False, "cases": out}
+
+
 # ---------------------------------------------------------------- own arm
 def run_own(args) -> None:
     import numpy as np
@@ -467,6 +515,7 @@ def run_own(args) -> None:
     if rank == 0:
         cb = cpu_baseline(min(args.cpu_sample, B))
         serving = None if args.no_serving else serving_sweep(g, ctx, torch)
+        precision = precision_form(ctx, torch, s)
         line = {
             "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": round(ms, 4),
@@ -490,6 +539,7 @@ def run_own(args) -> None:
             "e2e": e2e,
             "phase_correlate": pc,
             "serving": serving,
+            "precision_form": precision,
             "clocks": clk,
             "gpu_launches": launches_per_step * args.steps,
         }

@@ -45,6 +45,7 @@ _SIGNATURES = {
     "glsfft_fft_rows": (_ip, [_vp, _vp, _vp, _ip, _ip, _ip, _ip, _vp]),
     "glsfft_fft_cols": (_ip, [_vp, _vp, _vp, _ip, _ip, _ip, _ip, _vp]),
     "glsfft_fft2d_batched": (_ip, [_vp, _vp, _vp, _ip, _ip, _ip, _ip, _vp]),
+    "glsfft_fft2d_tc": (_ip, [_vp, _vp, _vp, _ip, _ip, _ip, _ip, _vp]),
     "glsfft_phase_correlate": (_ip, [_vp, _vp, _vp, _vp, _ip, _ip, _ip, _dp, _dp, _dp, _vp]),
     "glsfft_phase_correlate_async": (_ip, [_vp, _vp, _vp, _vp, _ip, _ip, _ip, _vp, _vp]),
     "glsfft_phase_correlate_surface": (_ip, [_vp, _vp, _sz, _vp]),
@@ -140,6 +141,12 @@ class Context:
                       flags: int = 0, stream: int = 0) -> None:
         check(lib().glsfft_fft2d_batched(self.handle, src, dst, count, rows, cols, flags, stream),
               "fft2d_batched")
+
+    def fft2d_tc(self, src: int, dst: int, count: int, rows: int, cols: int, flags: int = 0,
+                 stream: int = 0) -> None:
+        """Precision form: split-FP16 tensor-core four-step FFT (1024/4096 lines)."""
+        check(lib().glsfft_fft2d_tc(self.handle, src, dst, count, rows, cols, flags, stream),
+              "fft2d_tc")
 
     def fft_rows(self, src: int, dst: int, rows: int, cols: int, flags: int = 0,
                  stream: int = 0, count: int = 1) -> None:

@@ -19,10 +19,14 @@ using namespace glsfft;
 // e^{-2 pi i k/n} (k < n, n a power of two) in FP64 from an exact quadrant /
 // octant reduction, so that +-1, 0 and the pi/4 values come out exact and
 // symmetric, then one rounding to FP32.
-static float2 twiddle(long long k, long long n) {
+static void twiddle_d(long long k, long long n, double &re, double &im) {
     const double two_pi = 6.283185307179586476925286766559;
     k %= n;
-    if (n < 4) return make_float2(k == 0 ? 1.0f : -1.0f, 0.0f);
+    if (n < 4) {
+        re = k == 0 ? 1.0 : -1.0;
+        im = 0.0;
+        return;
+    }
     const long long q = (4 * k) / n;       // quadrant
     const long long r = k - q * (n / 4);   // position inside the quadrant
     double c, s;                           // cos, sin of 2 pi r / n
@@ -39,7 +43,70 @@ static float2 twiddle(long long k, long long n) {
         c = -s;
         s = t;
     }
-    return make_float2((float)c, (float)(-s));  // forward sign: cos - i sin
+    re = c;   // forward sign: cos - i sin
+    im = -s;
+}
+
+static float2 twiddle(long long k, long long n) {
+    double re, im;
+    twiddle_d(k, n, re, im);
+    return make_float2((float)re, (float)im);
+}
+
+// ---------------------------------------------- tensor-core form tables
+int glsfft::tc_tables_create(TcTables *t) {
+    const size_t f32_halves = 64 * 72, f64_halves = 128 * 136;  // 2N1 x (2N1 + 8)
+    const size_t bytes = 2 * (f32_halves + f64_halves) * sizeof(__half) +
+                         (1024 + 4096) * sizeof(float2) + 256;
+    std::vector<unsigned char> host(bytes, 0);
+    unsigned char *p = host.data();
+    __half *h32 = reinterpret_cast<__half *>(p), *l32 = h32 + f32_halves;
+    __half *h64 = l32 + f32_halves, *l64 = h64 + f64_halves;
+    float2 *tw1 = reinterpret_cast<float2 *>(
+        (reinterpret_cast<uintptr_t>(l64 + f64_halves) + 15) & ~uintptr_t(15));
+    float2 *tw4 = tw1 + 1024;
+    auto fill = [](__half *hi, __half *lo, int n1) {
+        const int stride = 2 * n1 + 8;
+        for (int r = 0; r < 2 * n1; r++)
+            for (int c = 0; c < 2 * n1; c++) {
+                double re, im;  // F[k][n] = e^{-2 pi i k n / n1}
+                twiddle_d((long long)(r % n1) * (c % n1), n1, re, im);
+                // [Fr -Fi; Fi Fr]
+                const double v = (r < n1) == (c < n1) ? re : (r < n1 ? -im : im);
+                const __half h = __double2half(v);
+                hi[r * stride + c] = h;
+                lo[r * stride + c] = __double2half(v - (double)__half2float(h));
+            }
+    };
+    fill(h32, l32, 32);
+    fill(h64, l64, 64);
+    for (int k1 = 0; k1 < 32; k1++)
+        for (int n2 = 0; n2 < 32; n2++) tw1[k1 * 32 + n2] = twiddle((long long)k1 * n2, 1024);
+    for (int k1 = 0; k1 < 64; k1++)
+        for (int n2 = 0; n2 < 64; n2++) tw4[k1 * 64 + n2] = twiddle((long long)k1 * n2, 4096);
+    void *d = nullptr;
+    cudaError_t e = cudaMalloc(&d, bytes);
+    if (e == cudaSuccess) e = cudaMemcpy(d, host.data(), bytes, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        if (d) cudaFree(d);
+        return cuda_status(e);
+    }
+    unsigned char *b = static_cast<unsigned char *>(d);
+    auto rebase = [&](const void *hp) { return b + (static_cast<const unsigned char *>(hp) - p); };
+    t->block = d;
+    t->f32_hi = reinterpret_cast<__half *>(rebase(h32));
+    t->f32_lo = reinterpret_cast<__half *>(rebase(l32));
+    t->f64_hi = reinterpret_cast<__half *>(rebase(h64));
+    t->f64_lo = reinterpret_cast<__half *>(rebase(l64));
+    t->tw1024 = reinterpret_cast<float2 *>(rebase(tw1));
+    t->tw4096 = reinterpret_cast<float2 *>(rebase(tw4));
+    return GLSFFT_SUCCESS;
+}
+
+void glsfft::tc_tables_destroy(TcTables *t) {
+    if (t->block) cudaFree(t->block);
+    *t = TcTables{};
 }
 
 // Per-pass tables (see tw_offset), for every radix R and every length
@@ -267,11 +334,14 @@ int glsfft_context_create(glsfft_context *out, int device) {
     if (e == cudaSuccess)
         e = cudaMemcpy(ctx->d_tw, tw.data(), sizeof(float2) * tw.size(), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMallocHost(&ctx->h_result, 8 * sizeof(double));
-    if (e != cudaSuccess) {
+    int st = cuda_status(e);
+    if (!st) st = tc_tables_create(&ctx->tc);
+    if (st) {
         cudaGetLastError();
         if (ctx->d_tw) cudaFree(ctx->d_tw);
+        if (ctx->h_result) cudaFreeHost(ctx->h_result);
         delete ctx;
-        return cuda_status(e);
+        return st;
     }
     *out = ctx;
     return GLSFFT_SUCCESS;
@@ -283,8 +353,43 @@ int glsfft_context_destroy(glsfft_context ctx) {
     if (ctx->ws) cudaFree(ctx->ws);
     if (ctx->d_tw) cudaFree(ctx->d_tw);
     if (ctx->h_result) cudaFreeHost(ctx->h_result);
+    tc_tables_destroy(&ctx->tc);
     delete ctx;
     return GLSFFT_SUCCESS;
+}
+
+int glsfft_fft2d_tc(glsfft_context ctx, const void *src, void *dst, int count, int rows,
+                    int cols, int flags, void *stream) {
+    int st = check_fft_args(src, dst, rows, cols, flags, false);
+    if (st) return st;
+    if (count < 1 || count > kMaxBatch) return GLSFFT_ERROR_INVALID_VALUE;
+    if ((rows != 1024 && rows != 4096) || (cols != 1024 && cols != 4096)) return GLSFFT_ERROR_SIZE;
+    if (!ctx) return GLSFFT_ERROR_INVALID_VALUE;
+    DeviceGuard g(ctx->device);
+    if (!g.ok()) return GLSFFT_ERROR_CUDA;
+    const bool inv = flags & GLSFFT_INVERSE, scale = flags & GLSFFT_SCALE,
+               shift = flags & GLSFFT_SHIFT;
+    const size_t bytes = (size_t)rows * cols * sizeof(float2);
+    cudaStream_t s = (cudaStream_t)stream;
+    PassArgs a{};
+    a.in0 = src;
+    a.out0 = dst;
+    a.rows = rows;
+    a.cols = cols;
+    a.scale = scale ? 1.0f / (float)cols : 1.0f;
+    a.flags = (inv ? PF_CONJ_IN : 0u) | (shift ? PF_SHIFT_COLS : 0u);
+    a.in_img_bytes = a.out_img_bytes = bytes;
+    cudaError_t e = launch_tc_lines(cols, true, a, ctx->tc, count, s);
+    if (e != cudaSuccess) return cuda_status(e);
+    PassArgs b{};
+    b.in0 = dst;
+    b.out0 = dst;
+    b.rows = rows;
+    b.cols = cols;
+    b.scale = scale ? 1.0f / (float)rows : 1.0f;
+    b.flags = (inv ? PF_CONJ_OUT : 0u) | (shift ? PF_SHIFT_ROWS : 0u);
+    b.in_img_bytes = b.out_img_bytes = bytes;
+    return cuda_status(launch_tc_lines(rows, false, b, ctx->tc, count, s));
 }
 
 int glsfft_context_set_budget(glsfft_context ctx, size_t bytes) {

@@ -5,6 +5,7 @@
 #include <stddef.h>
 
 #include "glsfft.h"
+#include "tc_internal.h"
 
 struct glsfft_context_s {
     int device = 0;
@@ -13,6 +14,7 @@ struct glsfft_context_s {
     size_t ws_bytes = 0;
     size_t budget = 0;          // 0 = unlimited
     double *h_result = nullptr; // pinned, 8 doubles
+    glsfft::TcTables tc;        // split-FP16 tensor-core form tables
     const float *surface = nullptr;  // last phaseCorrelate surface
     size_t surface_count = 0;
 };

@@ -1,0 +1,28 @@
+// tc_internal.h -- tables and launcher of the split-FP16 tensor-core form.
+#pragma once
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+#include "glsfft_internal.h"
+
+namespace glsfft {
+
+// Device tables, generated in FP64 on the host once per context:
+// real-ified DFT matrices [Fr -Fi; Fi Fr] of size 2*N1 split into FP16 hi/lo
+// (rows padded to 2*N1 + 8 halves), and the four-step twiddles
+// e^{-2 pi i k1 n2 / N} at [k1*N1 + n2].
+struct TcTables {
+    __half *f32_hi = nullptr, *f32_lo = nullptr;  // N1 = 32 (N = 1024)
+    __half *f64_hi = nullptr, *f64_lo = nullptr;  // N1 = 64 (N = 4096)
+    float2 *tw1024 = nullptr, *tw4096 = nullptr;
+    void *block = nullptr;  // one allocation holding all of the above
+};
+
+int tc_tables_create(TcTables *t);
+void tc_tables_destroy(TcTables *t);
+
+// 1-D FFTs of length n (1024 or 4096) of every row (rows = true) or column.
+cudaError_t launch_tc_lines(int n, bool rows, const PassArgs &a, const TcTables &t, int images,
+                            cudaStream_t s);
+
+}  // namespace glsfft

@@ -119,6 +119,17 @@ GLSFFT_API int glsfft_fft_rows(glsfft_context ctx, const void *src, void *dst, i
 GLSFFT_API int glsfft_fft_cols(glsfft_context ctx, const void *src, void *dst, int count,
                                int rows, int cols, int flags, void *stream);
 
+/*
+ * Precision form of the batched 2-D FFT (no reference counterpart): each
+ * 1024- or 4096-point line is a four-step FFT (32 x 32 or 64 x 64) whose two
+ * DFT stages run as complex matrix products on the tensor cores with FP16
+ * hi/lo split operands (hi*hi + hi*lo + lo*hi, FP32 accumulate, power-of-two
+ * block scaling), giving FP32-level error.  rows, cols in {1024, 4096};
+ * `count` back-to-back images like glsfft_fft2d_batched; same flags.
+ */
+GLSFFT_API int glsfft_fft2d_tc(glsfft_context ctx, const void *src, void *dst, int count,
+                               int rows, int cols, int flags, void *stream);
+
 typedef struct glsfft_batch_s *glsfft_batch;
 
 /*
