@@ -47,7 +47,12 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-serving", action="store_true", help="skip the serving sweep")
     p.add_argument("--profile-only", action="store_true",
-                   help="build the batch plan, run it warmup+1 times and exit (for ncu)")
+                   help="build the batch plan, run it warmup+1 times and exit (for ncu); "
+                        "the plan keeps its default schedule")
+    p.add_argument("--no-autotune", action="store_true",
+                   help="keep the batch plans' default schedules")
+    p.add_argument("--no-uneven", action="store_true",
+                   help="skip the 512-image uneven-size batch section")
     return p.parse_args()
 
 
@@ -318,6 +323,85 @@ def precision_form(ctx, torch, s) -> dict:
 
 
 # ---------------------------------------------------------------- own arm
+VARIANT_KERNELS = {0: "fft_batch_persistent", 1: "fft_batch_ws<1>", 2: "fft_batch_ws<2>"}
+
+
+def uneven_batch(g, ctx, torch, s, no_autotune: bool, n_images: int = 512, reps: int = 10) -> dict:
+    """512 CV_32FC2 images, sizes drawn with seed 3 from {128^2, 256^2, 512^2,
+    1024^2, 1024x2048} with weights {.3,.3,.2,.15,.05}, forward FFT: one
+    autotuned batch plan (one graph launch) vs the plain per-image path (one
+    glsfft_fft2d_c2c call per image).  Inputs uniform[-1,1) from a seeded
+    device generator; 1.4 GB of input, larger than L2."""
+    from glscv_gb300 import workloads as wl
+    shapes = wl.batch_sizes(n_images, seed=3)
+    offs, total = [], 0
+    for r, c in shapes:
+        offs.append(total)
+        total += (r * c + 31) // 32 * 32  # complex elements, 256-byte aligned
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(3)
+    pool_in = torch.empty(total, dtype=torch.complex64, device="cuda")
+    pool_in.view(torch.float32).uniform_(-1.0, 1.0, generator=gen)
+    pool_out = torch.empty_like(pool_in)
+    esz = 8
+    pin = [pool_in.data_ptr() + o * esz for o in offs]
+    pout = [pool_out.data_ptr() + o * esz for o in offs]
+    plan = g.Batch(ctx, pin, pout, shapes, (0,))
+    tune = None
+    if not no_autotune:
+        tt = time.perf_counter()
+        tune = plan.autotune(None, reps=5, stream=s)
+        tune["seconds"] = round(time.perf_counter() - tt, 3)
+    stream = torch.cuda.current_stream()
+
+    def timed(fn, k):
+        for _ in range(3):
+            fn()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(k):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / k
+
+    def plain():
+        for i, (r, c) in enumerate(shapes):
+            ctx.fft2d(pin[i], pout[i], r, c, 0, s)
+
+    batch_ms = timed(lambda: plan.execute(s), reps)
+    st = plan.status(s)
+    plain_ms = timed(plain, 3)
+    flops = sum(wl.fft_flops(r, c) for r, c in shapes)
+    alg = sum(wl.fft_bytes(r, c) for r, c in shapes)
+    peak, peak_kind = measured_peaks()
+    info = plan.info()
+    hist = {}
+    for r, c in shapes:
+        hist[f"{r}x{c}"] = hist.get(f"{r}x{c}", 0) + 1
+    out = {
+        "workload": f"{n_images} CV_32FC2 images, sizes drawn with seed 3 (rows x cols: count)",
+        "sizes": hist, "status": st, "persistent_images": info["persistent_images"],
+        "items": info["items"], "grid": info["grid"], "schedule": plan.schedule(),
+        "autotune": tune,
+        "batch": {"ms": round(batch_ms, 4), "gflops": round(flops / (batch_ms * 1e-3) / 1e9, 1),
+                  "alg_gbs": round(alg / (batch_ms * 1e-3) / 1e9, 1),
+                  "frac_of_hbm": round(alg / (batch_ms * 1e-3) / 1e9 / peak, 4),
+                  "peak_kind": peak_kind},
+        "plain_per_image": {"ms": round(plain_ms, 4),
+                            "gflops": round(flops / (plain_ms * 1e-3) / 1e9, 1),
+                            "launches": 2 * n_images},
+        "speedup_vs_plain": round(plain_ms / batch_ms, 3),
+        "alg_bytes": alg, "flops": flops,
+    }
+    plan.close()
+    del pool_in, pool_out
+    torch.cuda.empty_cache()
+    return out
+
+
 def run_own(args) -> None:
     import numpy as np
     import torch
@@ -360,6 +444,11 @@ def run_own(args) -> None:
     # the batch plan: every image forward then INVERSE|SCALE, one persistent
     # warp-specialised launch per step (graph: a counter memset + the kernel)
     plan = g.Batch(ctx, ptr_in, ptr_out, [(ROWS, COLS)] * B, (0, INV | SCALE))
+    tune = None
+    if not (args.no_autotune or args.profile_only):
+        tt = time.perf_counter()
+        tune = plan.autotune(None, reps=5, stream=s)
+        tune["seconds"] = round(time.perf_counter() - tt, 3)
     launches_per_step = 1
     ev = {}
     base_in, base_out = d_in.data_ptr(), d_out.data_ptr()
@@ -445,8 +534,9 @@ def run_own(args) -> None:
     alg_bytes = 4 * 16.0 * ROWS * COLS * B
     achieved = alg_bytes / (avg[dom] * 1e-3) / 1e9
     peak, peak_kind = measured_peaks()
-    kernel_name = f"fft_batch_ws<2> 1024x1024 x{B} fwd+inv"
-    traffic = traffic_per_launch(f"fft_batch_ws<2>x{B}")
+    kname = VARIANT_KERNELS[plan.schedule()["variant"]]
+    kernel_name = f"{kname} 1024x1024 x{B} fwd+inv"
+    traffic = traffic_per_launch(f"{kname}x{B}")
 
     # the same batch through the two-launch batched path and through the
     # plain per-image path (the >= 3x comparison)
@@ -516,13 +606,15 @@ def run_own(args) -> None:
         cb = cpu_baseline(min(args.cpu_sample, B))
         serving = None if args.no_serving else serving_sweep(g, ctx, torch)
         precision = precision_form(ctx, torch, s)
+        uneven = None if args.no_uneven else uneven_batch(g, ctx, torch, s, args.no_autotune)
         line = {
             "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": round(ms, 4),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic", "config": config(B, world),
-            "path": "batch plan: one CUDA-graph launch of the persistent warp-specialised "
-                    "kernel (TMA-staged tiles, (image, pass, tile) work queue) per step",
+            "path": "batch plan: one CUDA-graph launch of the persistent kernel "
+                    "((image, pass, tile) work queue; schedule picked by the autotuner) per step",
+            "autotune": tune,
             "plain_per_image": {"value": round(plain_value, 3), "unit": UNIT,
                                 "ms_per_step": round(plain_ms, 4),
                                 "speedup_of_value": round(value / plain_value, 3)},
@@ -540,6 +632,7 @@ def run_own(args) -> None:
             "phase_correlate": pc,
             "serving": serving,
             "precision_form": precision,
+            "uneven_batch": uneven,
             "clocks": clk,
             "gpu_launches": launches_per_step * args.steps,
         }

@@ -16,7 +16,7 @@ from pathlib import Path
 
 __all__ = [
     "lib", "GlsError", "Context", "DFT_INVERSE", "DFT_SCALE", "GLS_FFT_SHIFT",
-    "GLS_FFT_INVERSE", "GLS_FFT_SCALE", "LIB_PATH", "HEADER_PATHS",
+    "GLS_FFT_INVERSE", "GLS_FFT_SCALE", "LIB_PATH", "HEADER_PATHS", "schedule_available",
 ]
 
 PKG = Path(__file__).resolve().parent
@@ -60,6 +60,13 @@ _SIGNATURES = {
     "glsfft_batch_info": (_ip, [_vp, ctypes.POINTER(_ip), ctypes.POINTER(_ip),
                                 ctypes.POINTER(_ip)]),
     "glsfft_batch_inject_stall": (_ip, [_vp, ctypes.c_longlong]),
+    "glsfft_batch_get_schedule": (_ip, [_vp, ctypes.POINTER(_ip)]),
+    "glsfft_batch_autotune": (_ip, [_vp, ctypes.c_char_p, _ip, _vp, ctypes.POINTER(_ip), _dp]),
+    "glsfft_schedule_available": (_ip, [_ip, _ip, _ip]),
+    "glsfft_set_fft_schedule": (_ip, [_vp, _ip, _ip, _ip, _ip]),
+    "glsfft_get_fft_schedule": (_ip, [_vp, _ip, _ip, ctypes.POINTER(_ip), ctypes.POINTER(_ip)]),
+    "glsfft_autotune_fft2d": (_ip, [_vp, _ip, _ip, _ip, ctypes.c_char_p, _vp,
+                                    ctypes.POINTER(_ip), _dp]),
     "glsfft_batch_destroy": (_ip, [_vp]),
     "glsfft_server_create": (_ip, [_vp, _ip, _sz, ctypes.POINTER(_vp)]),
     "glsfft_server_add_reference": (_ip, [_vp, _vp, _vp, _ip, _ip, ctypes.POINTER(_ip)]),
@@ -184,6 +191,30 @@ class Context:
     def set_budget(self, nbytes: int) -> None:
         check(lib().glsfft_context_set_budget(self.handle, nbytes), "set_budget")
 
+    def set_fft_schedule(self, rows: int, cols: int, row_schedule: int, col_schedule: int) -> None:
+        check(lib().glsfft_set_fft_schedule(self.handle, rows, cols, row_schedule, col_schedule),
+              "set_fft_schedule")
+
+    def get_fft_schedule(self, rows: int, cols: int) -> tuple[int, int]:
+        r, c = _ip(), _ip()
+        check(lib().glsfft_get_fft_schedule(self.handle, rows, cols, ctypes.byref(r),
+                                            ctypes.byref(c)), "get_fft_schedule")
+        return r.value, c.value
+
+    def autotune_fft2d(self, rows: int, cols: int, count: int = 1, cache_path: str | None = None,
+                       stream: int = 0) -> dict:
+        res = (_ip * 3)()
+        ms = (ctypes.c_double * 2)()
+        path = cache_path.encode() if cache_path else None
+        check(lib().glsfft_autotune_fft2d(self.handle, rows, cols, count, path, stream, res, ms),
+              "autotune_fft2d")
+        return {"row_schedule": res[0], "col_schedule": res[1], "from_cache": bool(res[2]),
+                "ms": ms[0], "ms_default": ms[1]}
+
+
+def schedule_available(length: int, schedule: int, along_cols: bool) -> bool:
+    return bool(lib().glsfft_schedule_available(length, schedule, int(along_cols)))
+
 
 class Batch:
     """A batch plan (glsfft_batch): uneven-size images through 1-2 transforms,
@@ -223,6 +254,22 @@ class Batch:
 
     def inject_stall(self, wait_limit_ns: int) -> None:
         check(lib().glsfft_batch_inject_stall(self.handle, int(wait_limit_ns)), "inject_stall")
+
+    def schedule(self) -> dict:
+        out = (_ip * 4)()
+        check(lib().glsfft_batch_get_schedule(self.handle, out), "batch_get_schedule")
+        return {"variant": out[0], "claim_chunk": out[1], "claim_ahead": out[2],
+                "lag_items": out[3]}
+
+    def autotune(self, cache_path: str | None = None, reps: int = 5, stream: int = 0) -> dict:
+        res = (_ip * 6)()
+        ms = (ctypes.c_double * 2)()
+        path = cache_path.encode() if cache_path else None
+        check(lib().glsfft_batch_autotune(self.handle, path, reps, stream, res, ms),
+              "batch_autotune")
+        return {"variant": res[0], "claim_chunk": res[1], "claim_ahead": res[2],
+                "lag_items": res[3], "from_cache": bool(res[4]), "candidates": res[5],
+                "ms": ms[0], "ms_default": ms[1]}
 
     def close(self) -> None:
         if self.handle:

@@ -6,11 +6,16 @@
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
+#include <algorithm>
 #include <cstdint>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <deque>
+#include <map>
 #include <mutex>
 #include <new>
+#include <string>
 #include <vector>
 
 #include "batch_internal.h"
@@ -42,6 +47,7 @@ struct glsfft_batch_s {
     cudaGraphExec_t exec = nullptr;
     long long wait_limit_ns = 2000000000LL;
     size_t o_items = 0;
+    int lag_items = 0;  // the item order's lag (order_items)
 };
 
 namespace {
@@ -244,7 +250,8 @@ int glsfft_batch_create(glsfft_context ctx, int count, const void *const *srcs,
         plan->grid = grid_for(ctx->device, plan->variant);
         if (plan->grid <= 0) st = GLSFFT_ERROR_CUDA;
         std::vector<BatchItem> items;
-        if (!st) items = order_items(plan->images, plan->passes, kDefaultLagGrids * plan->grid);
+        plan->lag_items = kDefaultLagGrids * plan->grid;
+        if (!st) items = order_items(plan->images, plan->passes, plan->lag_items);
         plan->n_items = (int)items.size();
         const size_t ni = plan->images.size();
         const size_t b_tm = 128 * ni;
@@ -318,6 +325,7 @@ int glsfft_batch_set_variant(glsfft_batch plan, int variant) {
                                        cudaMemcpyHostToDevice);
             if (e != cudaSuccess) return cuda_status(e);
             plan->grid = grid;
+            plan->lag_items = kDefaultLagGrids * grid;
         }
     }
     plan->variant = variant;
@@ -336,6 +344,7 @@ int glsfft_batch_set_schedule(glsfft_batch plan, int claim_chunk, int claim_ahea
         cudaError_t e = cudaMemcpy(static_cast<char *>(plan->d_mem) + plan->o_items, items.data(),
                                    sizeof(BatchItem) * items.size(), cudaMemcpyHostToDevice);
         if (e != cudaSuccess) return cuda_status(e);
+        plan->lag_items = lag_blocks;
     }
     return capture(plan);
 }
@@ -387,6 +396,216 @@ int glsfft_batch_inject_stall(glsfft_batch plan, long long wait_limit_ns) {
     plan->wait_limit_ns = wait_limit_ns;
     plan->args.wait_limit_ns = wait_limit_ns;
     return capture(plan);
+}
+
+int glsfft_batch_get_schedule(glsfft_batch plan, int *out4) {
+    if (!plan || !out4) return GLSFFT_ERROR_INVALID_VALUE;
+    out4[0] = plan->variant;
+    out4[1] = plan->args.claim_chunk ? plan->args.claim_chunk : kDefaultClaimChunk;
+    out4[2] = plan->args.claim_ahead;
+    out4[3] = plan->lag_items;
+    return GLSFFT_SUCCESS;
+}
+
+int glsfft_batch_autotune(glsfft_batch plan, const char *cache_path, int reps, void *stream,
+                          int *result, double *ms) {
+    if (!plan || reps < 1 || reps > 1000) return GLSFFT_ERROR_INVALID_VALUE;
+    DeviceGuard g(plan->device);
+    if (!g.ok()) return GLSFFT_ERROR_CUDA;
+    glsfft_context ctx = plan->ctx;
+    cudaStream_t s = (cudaStream_t)stream;
+    int st = GLSFFT_SUCCESS;
+
+    // 1. per-size pass schedules of the images that get their own launches
+    std::map<std::pair<int, int>, int> other_sizes;
+    for (const auto &o : plan->others) other_sizes[{o.rows, o.cols}]++;
+    for (const auto &kv : other_sizes) {
+        st = glsfft_autotune_fft2d(ctx, kv.first.first, kv.first.second,
+                                   std::min(kv.second, 64), cache_path, stream, nullptr, nullptr);
+        if (st) return st;
+    }
+
+    int res[6] = {plan->variant, plan->args.claim_chunk, plan->args.claim_ahead, plan->lag_items,
+                  0, 0};
+    double t[2] = {0.0, 0.0};
+    if (plan->n_images == 0) {  // nothing persistent: re-record the per-size schedules
+        st = capture(plan);
+        if (!st && result) std::copy(res, res + 6, result);
+        if (!st && ms) std::copy(t, t + 2, ms);
+        return st;
+    }
+
+    // 2. the plan key: device, the persistent images' and the other images'
+    //    size histograms, the transform flags
+    auto histogram = [](const std::map<std::pair<int, int>, int> &h) {
+        std::string o;
+        for (const auto &kv : h) {
+            if (!o.empty()) o += ";";
+            o += std::to_string(kv.first.first) + "x" + std::to_string(kv.first.second) + "*" +
+                 std::to_string(kv.second);
+        }
+        return o;
+    };
+    std::map<std::pair<int, int>, int> pers;
+    for (const auto &im : plan->images) pers[{im.rows, im.cols}]++;
+    std::string flags;
+    for (int f : plan->flags) flags += (flags.empty() ? "" : ",") + std::to_string(f);
+    plan_cache::Pairs key = device_fields(plan->device);
+    key.push_back({"kind", plan_cache::quote("batch")});
+    key.push_back({"persistent", plan_cache::quote(histogram(pers))});
+    key.push_back({"others", plan_cache::quote(histogram(other_sizes))});
+    key.push_back({"flags", plan_cache::quote(flags)});
+
+    auto apply = [&](int variant, int chunk, int ahead, int lag_grids) {
+        int r = glsfft_batch_set_variant(plan, variant);
+        if (!r) r = glsfft_batch_set_schedule(plan, chunk, ahead, lag_grids * plan->grid);
+        return r;
+    };
+    plan_cache::Fields hit;
+    if (plan_cache::lookup(cache_path, plan_cache::as_fields(key), hit)) {
+        const int v = std::atoi(hit["variant"].c_str()), c = std::atoi(hit["claim_chunk"].c_str()),
+                  a = std::atoi(hit["claim_ahead"].c_str()),
+                  lg = std::atoi(hit["lag_grids"].c_str());
+        if (v >= BATCH_PLAIN && v <= BATCH_TMA_WS2 && c >= 1 && c <= 4 && (a == 0 || a == 1) &&
+            lg >= 1) {
+            st = apply(v, c, a, lg);
+            if (st) return st;
+            res[0] = v;
+            res[1] = c;
+            res[2] = a;
+            res[3] = plan->lag_items;
+            res[4] = 1;
+            t[0] = std::atof(hit["ms"].c_str());
+            t[1] = std::atof(hit["ms_default"].c_str());
+            if (result) std::copy(res, res + 6, result);
+            if (ms) std::copy(t, t + 2, ms);
+            return GLSFFT_SUCCESS;
+        }
+    }
+
+    // 3. a shadow plan of the same shapes, flags, pointer alignments and
+    //    src/dst aliasing on scratch buffers: the caller's images are not touched
+    struct Shadow {
+        int rows, cols;
+        uintptr_t src_off, dst_off;
+        bool alias;
+        size_t src_at, dst_at;
+    };
+    std::vector<Shadow> sh;
+    size_t total = 0;
+    auto take = [&](size_t bytes) {
+        const size_t at = total;
+        total += (bytes + 16 + 255) / 256 * 256;
+        return at;
+    };
+    auto add = [&](const void *src, const void *dst, int rows, int cols) {
+        Shadow x{rows, cols, reinterpret_cast<uintptr_t>(src) & 15,
+                 reinterpret_cast<uintptr_t>(dst) & 15, src == dst, 0, 0};
+        const size_t bytes = (size_t)rows * cols * sizeof(float2);
+        x.src_at = take(bytes);
+        x.dst_at = x.alias ? x.src_at : take(bytes);
+        sh.push_back(x);
+    };
+    for (const auto &im : plan->images) add(im.src, im.dst, im.rows, im.cols);
+    for (const auto &o : plan->others) add(o.src, o.dst, o.rows, o.cols);
+    if (ctx->budget && total > ctx->budget) return GLSFFT_ERROR_BUDGET;
+    char *scratch = nullptr;
+    cudaError_t e = cudaMalloc(&scratch, total);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return GLSFFT_ERROR_OUT_OF_MEMORY;
+    }
+    e = cudaMemsetAsync(scratch, 0x3f, total, s);  // finite values
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    st = cuda_status(e);
+    std::vector<const void *> ssrc;
+    std::vector<void *> sdst;
+    std::vector<int> srows, scols;
+    for (const auto &x : sh) {
+        ssrc.push_back(scratch + x.src_at + x.src_off);
+        sdst.push_back(scratch + x.dst_at + x.dst_off);
+        srows.push_back(x.rows);
+        scols.push_back(x.cols);
+    }
+    glsfft_batch shadow = nullptr;
+    if (!st)
+        st = glsfft_batch_create(ctx, (int)sh.size(), ssrc.data(), sdst.data(), srows.data(),
+                                 scols.data(), (int)plan->flags.size(), plan->flags.data(),
+                                 &shadow);
+    if (!st && shadow->n_images != plan->n_images) st = GLSFFT_ERROR_CUDA;  // routing differs
+
+    // 4. every schedule: variant x item-order lag (resident grids) x claim
+    //    chunk x claim-ahead (the plain variant has no claim knobs)
+    struct Cand {
+        int v, c, a, lg;
+        double ms;
+    };
+    std::vector<Cand> cands;
+    const int variants[3] = {BATCH_TMA_WS2, BATCH_TMA_WS1, BATCH_PLAIN};
+    const int lags[4] = {1, 2, 4, 8};
+    for (int v : variants) {
+        for (int lg : lags) {
+            for (int c = 1; c <= 4 && !st; c *= 2) {
+                if (v == BATCH_PLAIN && c != kDefaultClaimChunk) continue;
+                for (int a = 0; a <= 1 && !st; a++) {
+                    if (v == BATCH_PLAIN && a) continue;
+                    st = glsfft_batch_set_variant(shadow, v);
+                    if (!st) st = glsfft_batch_set_schedule(shadow, c, a, lg * shadow->grid);
+                    double m = 0.0;
+                    if (!st)
+                        st = time_median_ms([&]() { return glsfft_batch_execute(shadow, s); }, 2,
+                                            reps, s, &m);
+                    if (!st) {
+                        const int dev_st = glsfft_batch_status(shadow, s);
+                        if (dev_st == GLSFFT_ERROR_TIMEOUT) continue;  // not a usable schedule
+                        st = dev_st;
+                    }
+                    if (!st) cands.push_back(Cand{v, c, a, lg, m});
+                }
+            }
+        }
+    }
+    if (shadow) glsfft_batch_destroy(shadow);
+    cudaStreamSynchronize(s);
+    cudaFree(scratch);
+    cudaGetLastError();
+    if (st) return st;
+    if (cands.empty()) return GLSFFT_ERROR_TIMEOUT;
+
+    // 5. the fastest, unless the default schedule is within the keep margin
+    const Cand *best = &cands[0], *def = nullptr;
+    for (const auto &c : cands) {
+        if (c.ms < best->ms) best = &c;
+        if (c.v == BATCH_TMA_WS2 && c.c == kDefaultClaimChunk && c.a == 0 &&
+            c.lg == kDefaultLagGrids)
+            def = &c;
+    }
+    if (def && best->ms > def->ms * 0.99) best = def;
+    st = apply(best->v, best->c, best->a, best->lg);
+    if (st) return st;
+    res[0] = best->v;
+    res[1] = best->c;
+    res[2] = best->a;
+    res[3] = plan->lag_items;
+    res[5] = (int)cands.size();
+    t[0] = best->ms;
+    t[1] = def ? def->ms : 0.0;
+    if (cache_path && *cache_path) {
+        key.push_back({"variant", std::to_string(best->v)});
+        key.push_back({"claim_chunk", std::to_string(best->c)});
+        key.push_back({"claim_ahead", std::to_string(best->a)});
+        key.push_back({"lag_grids", std::to_string(best->lg)});
+        char b[64];
+        std::snprintf(b, sizeof b, "%.6g", t[0]);
+        key.push_back({"ms", b});
+        std::snprintf(b, sizeof b, "%.6g", t[1]);
+        key.push_back({"ms_default", b});
+        key.push_back({"candidates", std::to_string(cands.size())});
+        if (!plan_cache::append(cache_path, key)) st = GLSFFT_ERROR_IO;
+    }
+    if (result) std::copy(res, res + 6, result);
+    if (ms) std::copy(t, t + 2, ms);
+    return st;
 }
 
 int glsfft_batch_destroy(glsfft_batch plan) {

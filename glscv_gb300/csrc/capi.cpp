@@ -187,6 +187,9 @@ int glsfft::fft2d_launch(glsfft_context ctx, const void *src, void *dst, int row
     const bool do_rows = cols > 1 || rows == 1 || real_in;
     const bool do_cols = rows > 1;
     const size_t px = (size_t)rows * cols;
+    FftSchedule sc{};
+    const auto it = ctx->sched.find(sched_key(rows, cols));
+    if (it != ctx->sched.end()) sc = it->second;
     if (do_rows) {
         PassArgs a{};
         a.in0 = src;
@@ -199,7 +202,8 @@ int glsfft::fft2d_launch(glsfft_context ctx, const void *src, void *dst, int row
         a.tw = ctx->d_tw;
         a.in_img_bytes = px * (real_in ? sizeof(float) : sizeof(float2));
         a.out_img_bytes = px * sizeof(float2);
-        cudaError_t e = launch_rows(cols, real_in ? LD_R1 : LD_C2, ST_C2, a, count, s);
+        cudaError_t e = real_in ? launch_rows(cols, LD_R1, ST_C2, a, count, s)
+                                : launch_rows_sched(cols, sc.row, a, count, s);
         if (e != cudaSuccess) return cuda_status(e);
     }
     if (do_cols) {
@@ -213,7 +217,7 @@ int glsfft::fft2d_launch(glsfft_context ctx, const void *src, void *dst, int row
                   (shift ? PF_SHIFT_ROWS : 0u);
         a.tw = ctx->d_tw;
         a.in_img_bytes = a.out_img_bytes = px * sizeof(float2);
-        cudaError_t e = launch_cols(rows, LD_C2, ST_C2, a, count, s);
+        cudaError_t e = launch_cols_sched(rows, sc.col, a, count, s);
         if (e != cudaSuccess) return cuda_status(e);
     }
     return GLSFFT_SUCCESS;
@@ -307,11 +311,12 @@ const char *glsfft_status_string(int status) {
     case GLSFFT_ERROR_NOALLOC_LIMIT:
         return "rows*cols exceeds the static scratch of glsfft_phase_correlate_noalloc "
                "(GLSFFT_NOALLOC_MAX_PIXELS)";
+    case GLSFFT_ERROR_IO: return "the plan cache file could not be written";
     default: return "unknown status";
     }
 }
 
-int glsfft_version(void) { return 100; }
+int glsfft_version(void) { return 200; }
 
 int glsfft_context_create(glsfft_context *out, int device) {
     if (!out) return GLSFFT_ERROR_INVALID_VALUE;
@@ -444,8 +449,11 @@ static int one_pass(glsfft_context ctx, const void *src, void *dst, int count, i
               ((flags & GLSFFT_SHIFT) ? (along_rows ? PF_SHIFT_COLS : PF_SHIFT_ROWS) : 0u);
     a.tw = ctx->d_tw;
     a.in_img_bytes = a.out_img_bytes = (size_t)rows * cols * sizeof(float2);
-    cudaError_t e = along_rows ? launch_rows(n, LD_C2, ST_C2, a, count, s)
-                               : launch_cols(n, LD_C2, ST_C2, a, count, s);
+    FftSchedule sc{};
+    const auto it = ctx->sched.find(sched_key(rows, cols));
+    if (it != ctx->sched.end()) sc = it->second;
+    cudaError_t e = along_rows ? launch_rows_sched(n, sc.row, a, count, s)
+                               : launch_cols_sched(n, sc.col, a, count, s);
     return cuda_status(e);
 }
 

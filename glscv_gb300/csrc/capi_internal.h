@@ -4,7 +4,12 @@
 #include <cuda_runtime.h>
 #include <stddef.h>
 
+#include <functional>
+#include <map>
+
 #include "glsfft.h"
+#include "plan_cache.h"
+#include "sched_internal.h"
 #include "tc_internal.h"
 
 struct glsfft_context_s {
@@ -17,6 +22,9 @@ struct glsfft_context_s {
     glsfft::TcTables tc;        // split-FP16 tensor-core form tables
     const float *surface = nullptr;  // last phaseCorrelate surface
     size_t surface_count = 0;
+    // per image size (sched_key): the pass schedules the complex 2-D FFT
+    // launches use; sizes not listed run schedule 0
+    std::map<long long, glsfft::FftSchedule> sched;
 };
 
 namespace glsfft {
@@ -46,6 +54,14 @@ constexpr int kMaxBatch = 65535;  // grid y extent
 int poc_launch(const float2 *tw, const float *src1, const float *src2, const float *window,
                int rows, int cols, int box, float2 *f1, float2 *f2, float *surface,
                unsigned long long *key, double *d_result, cudaStream_t s);
+
+// ------------------------------------------------------------- autotuner
+// The fields that identify the device a tuning was measured on.
+plan_cache::Pairs device_fields(int device);
+// Median of `reps` CUDA-event-timed runs of fn on stream s, after `warm`
+// untimed runs.  fn returns a glsfft status; the first failure is returned.
+int time_median_ms(const std::function<int()> &fn, int warm, int reps, cudaStream_t s,
+                   double *ms);
 
 // phaseCorrelate workspace: f1 | f2 (complex) | surface (float) | key | result
 inline size_t poc_key_offset(int rows, int cols) {

@@ -34,18 +34,24 @@ __device__ __forceinline__ float2 cconj(float2 a) { return make_float2(a.x, -a.y
 __device__ __forceinline__ float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
 
 // --------------------------------------------------------- radix schedule
+// mb = log2 of the largest radix allowed (4: radix <= 16, the default; 3:
+// radix <= 8, one more pass for most lengths but half the registers).
 __host__ __device__ constexpr int ilog2c(int n) { return n <= 1 ? 0 : 1 + ilog2c(n >> 1); }
-__host__ __device__ constexpr int num_passes(int n) {
-    return ilog2c(n) == 0 ? 0 : (ilog2c(n) <= 4 ? 1 : (ilog2c(n) + 3) / 4);
+__host__ __device__ constexpr int num_passes(int n, int mb = 4) {
+    return ilog2c(n) == 0 ? 0 : (ilog2c(n) <= mb ? 1 : (ilog2c(n) + mb - 1) / mb);
 }
-__host__ __device__ constexpr int pass_bits(int n, int p) {
-    return ilog2c(n) / num_passes(n) + (p < ilog2c(n) % num_passes(n) ? 1 : 0);
+__host__ __device__ constexpr int pass_bits(int n, int p, int mb = 4) {
+    return ilog2c(n) / num_passes(n, mb) + (p < ilog2c(n) % num_passes(n, mb) ? 1 : 0);
 }
-__host__ __device__ constexpr int pass_radix(int n, int p) { return 1 << pass_bits(n, p); }
-__host__ __device__ constexpr int pass_span(int n, int p) {
-    return p == 0 ? 1 : pass_span(n, p - 1) * pass_radix(n, p - 1);
+__host__ __device__ constexpr int pass_radix(int n, int p, int mb = 4) {
+    return 1 << pass_bits(n, p, mb);
 }
-__host__ __device__ constexpr int max_radix(int n) { return num_passes(n) == 0 ? 1 : pass_radix(n, 0); }
+__host__ __device__ constexpr int pass_span(int n, int p, int mb = 4) {
+    return p == 0 ? 1 : pass_span(n, p - 1, mb) * pass_radix(n, p - 1, mb);
+}
+__host__ __device__ constexpr int max_radix(int n, int mb = 4) {
+    return num_passes(n, mb) == 0 ? 1 : pass_radix(n, 0, mb);
+}
 
 // ------------------------------------------- multiply by w_R^K = e^{-2 pi i K/R}
 // Exact special cases for multiples of pi/4; cos/sin(pi/8) constants otherwise.
@@ -165,12 +171,12 @@ struct Strided {
 
 // Sm: shared-memory accessor (at(pos) -> float2*, KW) for this thread's line.
 // tw: the per-pass twiddle tables above.
-template <int N, int E, class Sync = SyncBlock>
+template <int N, int E, class Sync = SyncBlock, int MB = 4>
 struct LineFft {
     static_assert((N & (N - 1)) == 0 && N >= 1 && N <= 8192, "N must be a power of two");
     static_assert(N == 1 || (N % E) == 0, "E must divide N");
     static constexpr int T = (N >= E) ? N / E : 1;
-    static constexpr int P = num_passes(N);
+    static constexpr int P = num_passes(N, MB);
 
     template <class Sm>
     __device__ __forceinline__ static void run(float2 (&x)[E], int t, Sm sm,
@@ -183,8 +189,8 @@ struct LineFft {
                                                 const float2 *__restrict__ tw) {
         if constexpr (p < P) {
             [[maybe_unused]] const Sync sync{};
-            constexpr int R = pass_radix(N, p);
-            constexpr int Ns = pass_span(N, p);
+            constexpr int R = pass_radix(N, p, MB);
+            constexpr int Ns = pass_span(N, p, MB);
             constexpr int S = E / R;
             constexpr bool last = (Ns * R == N);
             static_assert(E % R == 0, "E must be a multiple of every radix");

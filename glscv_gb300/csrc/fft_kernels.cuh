@@ -100,11 +100,12 @@ __device__ __forceinline__ float2 load_elem(const void *img, const float *win, s
 }
 
 // ------------------------------------------------------------- row pass
-// Block: LINES rows x T threads.  blockIdx.y selects the image.
-template <int N, int E, int LINES, int LD, int ST>
+// Block: LINES rows x T threads.  blockIdx.y selects the image.  MB bounds
+// the radix (fft_device.cuh).
+template <int N, int E, int LINES, int LD, int ST, int MB = 4>
 __global__ void __launch_bounds__(LINES *LineFft<N, E>::T)
     fft_rows_kernel(PassArgs a) {
-    using F = LineFft<N, E>;
+    using F = LineFft<N, E, SyncBlock, MB>;
     constexpr int T = F::T;
     extern __shared__ float4 smem_raw[];
     float2 *smem = reinterpret_cast<float2 *>(smem_raw);
@@ -151,10 +152,10 @@ __global__ void __launch_bounds__(LINES *LineFft<N, E>::T)
 
 // ---------------------------------------------------------- column pass
 // Block: W adjacent columns x T threads, column index fastest.
-template <int N, int E, int W, int LD, int ST>
+template <int N, int E, int W, int LD, int ST, int MB = 4>
 __global__ void __launch_bounds__(W *LineFft<N, E>::T)
     fft_cols_kernel(PassArgs a) {
-    using F = LineFft<N, E>;
+    using F = LineFft<N, E, SyncBlock, MB>;
     constexpr int T = F::T;
     extern __shared__ float4 smem_raw[];
     float2 *smem = reinterpret_cast<float2 *>(smem_raw);

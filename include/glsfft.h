@@ -51,7 +51,8 @@ enum glsfft_status {
     GLSFFT_ERROR_BUDGET = 7,        /* workspace would exceed the context's HBM budget */
     GLSFFT_ERROR_TIMEOUT = 8,       /* a bounded device-side wait expired */
     GLSFFT_ERROR_SHAPE = 9,         /* inputs of different shapes */
-    GLSFFT_ERROR_NOALLOC_LIMIT = 10 /* rows*cols above GLSFFT_NOALLOC_MAX_PIXELS */
+    GLSFFT_ERROR_NOALLOC_LIMIT = 10, /* rows*cols above GLSFFT_NOALLOC_MAX_PIXELS */
+    GLSFFT_ERROR_IO = 11             /* the plan cache file could not be written */
 };
 
 typedef struct glsfft_context_s *glsfft_context;
@@ -130,6 +131,46 @@ GLSFFT_API int glsfft_fft_cols(glsfft_context ctx, const void *src, void *dst, i
 GLSFFT_API int glsfft_fft2d_tc(glsfft_context ctx, const void *src, void *dst, int count,
                                int rows, int cols, int flags, void *stream);
 
+/*
+ * Pass schedules of the plain path (no reference counterpart: glsCV runs
+ * one fixed radix-4 schedule, glsFft.cpp:494-671).  The complex row pass and
+ * column pass each have schedules 0..4 per line length: 0 the default;
+ * 1 half the elements per thread with the radix bound lowered to match;
+ * 2 twice the elements per thread; 3 / 4 half / twice the lines or columns
+ * per block.  All compute the same transform (rounding differs with the
+ * radix order, within the FP32 error bound).  Schedules other than 0 exist
+ * for lengths 64..4096 where the block fits the SM.
+ */
+#define GLSFFT_PASS_SCHEDULES 5
+/* 1 when `schedule` exists for a row pass (along_cols = 0) or column pass
+ * (along_cols = 1) of line length `length`, else 0. */
+GLSFFT_API int glsfft_schedule_available(int length, int schedule, int along_cols);
+
+/* Pass schedules that glsfft_fft2d_c2c, glsfft_fft2d_batched, the single
+ * pass entry points and batch plans' own-launch images use for complex
+ * rows x cols images on this context (default 0, 0). */
+GLSFFT_API int glsfft_set_fft_schedule(glsfft_context ctx, int rows, int cols, int row_schedule,
+                                       int col_schedule);
+GLSFFT_API int glsfft_get_fft_schedule(glsfft_context ctx, int rows, int cols,
+                                       int *row_schedule, int *col_schedule);
+
+/*
+ * Autotuner of the plain path for one image size: times every available
+ * schedule of the row pass and of the column pass over `count` images of
+ * rows x cols (median of 7 launches after 2, CUDA events on `stream`) on
+ * scratch buffers it allocates and frees, and sets the fastest of each
+ * (glsfft_set_fft_schedule) unless schedule 0 is within 1% of it.  With
+ * cache_path set, the choice is looked up in / appended to that plan cache
+ * file (one JSON object per line, keyed by device name, SM count, compute
+ * capability, driver, runtime and library versions, rows, cols, count); a
+ * hit is applied without timing.  result[3] = {row schedule, column
+ * schedule, 1 if from the cache}; ms[2] = {chosen, schedule 0}: row plus
+ * column pass time of one launch each.  Either may be NULL.
+ */
+GLSFFT_API int glsfft_autotune_fft2d(glsfft_context ctx, int rows, int cols, int count,
+                                     const char *cache_path, void *stream, int *result,
+                                     double *ms);
+
 typedef struct glsfft_batch_s *glsfft_batch;
 
 /*
@@ -190,6 +231,29 @@ GLSFFT_API int glsfft_batch_info(glsfft_batch plan, int *persistent_images, int 
  * next execution reports GLSFFT_ERROR_TIMEOUT instead of finishing cleanly.
  */
 GLSFFT_API int glsfft_batch_inject_stall(glsfft_batch plan, long long wait_limit_ns);
+
+/* The plan's current schedule: {variant, claim_chunk, claim_ahead, lag_items}. */
+GLSFFT_API int glsfft_batch_get_schedule(glsfft_batch plan, int *schedule4);
+
+/*
+ * Autotuner of a batch plan (no reference counterpart).  First the images
+ * that get their own pass launches have their per-size pass schedules tuned
+ * (glsfft_autotune_fft2d).  Then every persistent-kernel schedule -- variant
+ * (GLSFFT_BATCH_*) x item-order lag (1, 2, 4, 8 resident grids) x claim
+ * chunk (1, 2, 4) x claim-ahead (0, 1) -- is timed, `reps` graph launches
+ * each (median, CUDA events on `stream`), on a shadow plan of the same
+ * shapes, flags, alignments and aliasing over scratch buffers, so the
+ * plan's own images are never read or written.  The fastest is applied to
+ * the plan unless the default schedule is within 1% of it.  With cache_path
+ * set, the choice is looked up in / appended to that plan cache file
+ * (keyed by device, driver, library version, the plan's size histograms and
+ * flags); a hit is applied without timing.
+ * result[6] = {variant, claim_chunk, claim_ahead, lag_items, 1 if from the
+ * cache, candidates timed}; ms[2] = {chosen, default} per execution.
+ * Either may be NULL.
+ */
+GLSFFT_API int glsfft_batch_autotune(glsfft_batch plan, const char *cache_path, int reps,
+                                     void *stream, int *result, double *ms);
 
 GLSFFT_API int glsfft_batch_destroy(glsfft_batch plan);
 

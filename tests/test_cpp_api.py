@@ -50,3 +50,16 @@ def test_arena_allocator_host_unit(tmp_path):
     assert res.returncode == 0, res.stderr
     run = subprocess.run([str(out)], capture_output=True, text=True, timeout=60)
     assert run.returncode == 0 and "ALL OK" in run.stdout, run.stdout
+
+
+def test_plan_cache_host_unit(tmp_path):
+    """The autotuner's plan cache file format and lookup, compiled without CUDA."""
+    src = ROOT / "tests" / "cpp" / "test_plan_cache.cpp"
+    out = tmp_path / "test_plan_cache"
+    res = subprocess.run(["g++", "-std=c++17", "-O1", "-Wall",
+                          f"-I{ROOT / 'glscv_gb300' / 'csrc'}", str(src), "-o", str(out)],
+                         capture_output=True, text=True)
+    assert res.returncode == 0, res.stderr
+    run = subprocess.run([str(out), str(tmp_path / "cache.jsonl")], capture_output=True,
+                         text=True, timeout=60)
+    assert run.returncode == 0 and "ALL OK" in run.stdout, run.stdout
