@@ -371,7 +371,7 @@ GLSFFT_API int glsfft_server_destroy(glsfft_server server);
  * surface and the argmax word: 20 * rows * cols bytes) is one statically
  * sized device array of the library, so rows * cols must not exceed
  * GLSFFT_NOALLOC_MAX_PIXELS (GLSFFT_ERROR_NOALLOC_LIMIT otherwise).  That
- * array (5 MiB) and a 64 KiB twiddle table are held on every GPU that loads
+ * array (5 MiB) and a 256 KiB twiddle table are held on every GPU that loads
  * the library until the process exits.
  *
  * The first call on a device (the current device) sets up: it looks up the
