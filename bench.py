@@ -339,7 +339,8 @@ def precision_form(ctx, torch, s) -> dict:
 
 
 # ---------------------------------------------------------------- own arm
-VARIANT_KERNELS = {0: "fft_batch_persistent", 1: "fft_batch_ws<1>", 2: "fft_batch_ws<2>"}
+VARIANT_KERNELS = {0: "fft_batch_persistent", 1: "fft_batch_ws<1,3>", 2: "fft_batch_ws<2,3>",
+                   3: "fft_batch_ws<3,2>"}
 
 
 def uneven_batch(g, ctx, torch, s, no_autotune: bool, n_images: int = 512, reps: int = 10) -> dict:

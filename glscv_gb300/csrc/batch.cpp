@@ -106,7 +106,7 @@ std::vector<BatchItem> order_items(const std::vector<BatchImage> &ims,
 
 int grid_for(int device, int variant) {
     if (variant == BATCH_PLAIN) return batch_persistent_grid(device);
-    return batch_ws_grid(device, variant == BATCH_TMA_WS2 ? 2 : 1);
+    return batch_ws_grid(device, variant);  // WS1..WS3: 1..3 blocks per SM
 }
 
 int record(glsfft_batch plan, cudaStream_t s) {
@@ -118,7 +118,7 @@ int record(glsfft_batch plan, cudaStream_t s) {
         if (plan->variant == BATCH_PLAIN)
             e = launch_batch_persistent(plan->args, plan->grid, s);
         else
-            e = launch_batch_ws(plan->args, plan->grid, plan->variant == BATCH_TMA_WS2 ? 2 : 1, s);
+            e = launch_batch_ws(plan->args, plan->grid, plan->variant, s);
         if (e != cudaSuccess) return cuda_status(e);
     }
     for (const auto &o : plan->others) {
@@ -310,7 +310,7 @@ int glsfft_batch_create(glsfft_context ctx, int count, const void *const *srcs,
 }
 
 int glsfft_batch_set_variant(glsfft_batch plan, int variant) {
-    if (!plan || variant < BATCH_PLAIN || variant > BATCH_TMA_WS2) return GLSFFT_ERROR_INVALID_VALUE;
+    if (!plan || variant < BATCH_PLAIN || variant > BATCH_TMA_WS3) return GLSFFT_ERROR_INVALID_VALUE;
     DeviceGuard g(plan->device);
     if (!g.ok()) return GLSFFT_ERROR_CUDA;
     if (plan->n_images > 0) {
@@ -466,7 +466,7 @@ int glsfft_batch_autotune(glsfft_batch plan, const char *cache_path, int reps, v
         const int v = std::atoi(hit["variant"].c_str()), c = std::atoi(hit["claim_chunk"].c_str()),
                   a = std::atoi(hit["claim_ahead"].c_str()),
                   lg = std::atoi(hit["lag_grids"].c_str());
-        if (v >= BATCH_PLAIN && v <= BATCH_TMA_WS2 && c >= 1 && c <= 4 && (a == 0 || a == 1) &&
+        if (v >= BATCH_PLAIN && v <= BATCH_TMA_WS3 && c >= 1 && c <= 4 && (a == 0 || a == 1) &&
             lg >= 1) {
             st = apply(v, c, a, lg);
             if (st) return st;
@@ -541,7 +541,7 @@ int glsfft_batch_autotune(glsfft_batch plan, const char *cache_path, int reps, v
         double ms;
     };
     std::vector<Cand> cands;
-    const int variants[3] = {BATCH_TMA_WS2, BATCH_TMA_WS1, BATCH_PLAIN};
+    const int variants[4] = {BATCH_TMA_WS2, BATCH_TMA_WS3, BATCH_TMA_WS1, BATCH_PLAIN};
     const int lags[4] = {1, 2, 4, 8};
     for (int v : variants) {
         for (int lg : lags) {

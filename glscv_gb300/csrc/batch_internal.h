@@ -58,7 +58,7 @@ struct BatchArgs {
 // shared-memory ring; eight compute warps run the FFT and store).
 // The warp-specialised kernel comes compiled for 1 and for 2 blocks per SM
 // (at 2, nine warps per block cap registers at 96 and the FFT spills a little).
-enum { BATCH_PLAIN = 0, BATCH_TMA_WS1 = 1, BATCH_TMA_WS2 = 2 };
+enum { BATCH_PLAIN = 0, BATCH_TMA_WS1 = 1, BATCH_TMA_WS2 = 2, BATCH_TMA_WS3 = 3 };
 
 cudaError_t launch_batch_persistent(const BatchArgs &a, int grid, cudaStream_t s);
 int batch_persistent_grid(int device);  // blocks that fit on the device at once

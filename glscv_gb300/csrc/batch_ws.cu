@@ -11,13 +11,17 @@
 //     reference's separate tiled/untiled copy passes (glsCV/glsCopy.cpp).
 // Completion of each copy lands on the stage's "full" mbarrier.  The compute
 // warps read their 16 values per thread from the stage, run the Stockham
-// passes (exchanging through the same buffer), store to global memory, and
-// arrive on the stage's "stored" mbarrier.  The producer then publishes the
-// tile (release fence + counter) and refills the stage.  Items are published
-// in order, and the producer keeps publishing finished tiles while it waits
-// on a dependency, so no block ever holds back the work another waits for.
-// Every wait is bounded: on expiry the block records GLSFFT_ERROR_TIMEOUT,
-// lets the compute warps drain, waits for its own copies and exits.
+// passes (exchanging through the same buffer), write the results back into
+// the stage in the image's layout and arrive on the stage's "computed"
+// mbarrier.  The producer then writes the tile out with the TMA as well (one
+// cp.async.bulk for a rows tile, 2-D tensor boxes for a columns tile), so the
+// compute warps issue no global stores.  Before the stage is refilled the
+// store's bulk group must be complete; the producer then publishes the tile
+// (release fence + counter).  Items are stored and published in order, and
+// the producer completes and publishes every stored tile while it waits on a
+// dependency, so no block ever holds back the work another waits for.  Every
+// wait is bounded: on expiry the block records GLSFFT_ERROR_TIMEOUT, lets
+// the compute warps drain, waits for its own copies and exits.
 #include <cuda.h>
 
 #include "batch_internal.h"
@@ -29,7 +33,6 @@ namespace glsfft {
 
 namespace {
 
-constexpr int kStages = 3;
 constexpr int kCompute = 256;                      // compute threads
 constexpr int kBlock = kCompute + 32;              // + producer warp
 constexpr int kStageElems = 4352;                  // padded_count(4096)
@@ -43,13 +46,30 @@ struct StageInfo {
     int pad[5];
 };
 
+// Items stored but not yet published keep their (image, pass) here, since
+// their stage may already hold a later item.
+constexpr int kPubRing = 8;
+
+template <int ST>
 struct WsShared {
-    unsigned long long full[kStages];
-    unsigned long long stored[kStages];
-    StageInfo info[kStages];
+    unsigned long long full[ST];
+    unsigned long long computed[ST];
+    StageInfo info[ST];
+    int pub_image[kPubRing];
+    int pub_pass[kPubRing];
 };
 
-constexpr size_t kWsSmem = kStages * kStageBytes + sizeof(WsShared) + 128;
+// Shared-memory copy of the twiddle tables of the current line length, for
+// lengths 32..1024 (longer lines read the global tables).
+constexpr int kTwCacheMax = 1024;
+constexpr int kTwCacheF4 = tw_smem_float4(kTwCacheMax);
+__host__ __device__ constexpr bool tw_cached(int n) { return n >= 32 && n <= kTwCacheMax; }
+
+// dynamic shared memory of a block with ST stages
+template <int ST>
+constexpr size_t ws_smem() {
+    return ST * kStageBytes + kTwCacheF4 * sizeof(float4) + sizeof(WsShared<ST>) + 128;
+}
 
 __device__ __forceinline__ unsigned smem_u32(const void *p) {
     return (unsigned)__cvta_generic_to_shared(p);
@@ -115,6 +135,31 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, unsigned by
         "l"(src), "r"(bytes), "r"(smem_u32(bar))
         : "memory");
 }
+// shared -> global bulk copies, tracked by bulk groups of the issuing thread
+__device__ __forceinline__ void bulk_s2g(void *dst, const void *src, unsigned bytes) {
+    asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst),
+                 "r"(smem_u32(src)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void tensor2d_s2g(const void *tmap, int x, int y, const void *src) {
+    asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%1, %2}], [%3];" ::"l"(
+                     tmap),
+                 "r"(x), "r"(y), "r"(smem_u32(src))
+                 : "memory");
+}
+__device__ __forceinline__ void bulk_commit() {
+    asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+}
+// wait until at most K of this thread's most recent bulk groups are pending
+// (all of their writes done), or have at least finished reading their source
+template <int K>
+__device__ __forceinline__ void bulk_wait() {
+    asm volatile("cp.async.bulk.wait_group %0;" ::"n"(K) : "memory");
+}
+template <int K>
+__device__ __forceinline__ void bulk_wait_read() {
+    asm volatile("cp.async.bulk.wait_group.read %0;" ::"n"(K) : "memory");
+}
 __device__ __forceinline__ void tensor2d_g2s(void *dst, const void *tmap, int x, int y,
                                              unsigned long long *bar) {
     asm volatile(
@@ -125,9 +170,22 @@ __device__ __forceinline__ void tensor2d_g2s(void *dst, const void *tmap, int x,
 }
 
 // ------------------------------------------------------------ compute side
+// the line engine with the shared-memory tables where the length has them
+template <int N, class Sm>
+__device__ __forceinline__ void ws_line(float2 (&x)[16 < N ? 16 : N], int t, Sm sm,
+                                        const float2 *tw, const float4 *twc) {
+    constexpr int E = 16 < N ? 16 : N;
+    if constexpr (tw_cached(N)) {
+        static_assert(tw_smem_ok(N) && tw_smem_float4(N) <= kTwCacheF4, "twiddle cache layout");
+        LineFft<N, E, SyncCompute256>::run(x, t, sm, SmemTw<N>{twc});
+    } else {
+        LineFft<N, E, SyncCompute256>::run(x, t, sm, tw);
+    }
+}
+
 template <int N>
 __device__ __forceinline__ void ws_rows(float2 *stage, const StageInfo &in, const float2 *tw,
-                                        int tid) {
+                                        const float4 *twc, int tid) {
     constexpr int E = 16, T = N / E, LINES = kCompute / T;
     const int l = tid / T, t = tid % T;
     const int row = in.tile * LINES + l;
@@ -139,14 +197,17 @@ __device__ __forceinline__ void ws_rows(float2 *stage, const StageInfo &in, cons
     for (int m = 0; m < E; m++) x[m] = active ? sp[m * T] : make_float2(0.f, 0.f);
     conj_line(x, cin);
     SyncCompute256{}();  // the exchanges below overwrite the staged tile
-    LineFft<N, E, SyncCompute256>::run(x, t, RowSm{stage + l * padded_count(N)}, tw);
+    ws_line<N>(x, t, RowSm{stage + l * padded_count(N)}, tw, twc);
     finish_line(x, in.scale ? 1.0f / (float)N : 1.0f, cout);
-    if (active) store_line<N, E, T>(in.dst + (size_t)row * N, 1, x, t, in.flags & PF_SHIFT_COLS);
+    // results back into the stage as the tile's rows, contiguous, for the
+    // producer's bulk store (after every thread's last exchange read)
+    SyncCompute256{}();
+    if (active) store_line<N, E, T>(stage + l * N, 1, x, t, in.flags & PF_SHIFT_COLS);
 }
 
 template <int N>
 __device__ __forceinline__ void ws_cols(float2 *stage, const StageInfo &in, const float2 *tw,
-                                        int tid) {
+                                        const float4 *twc, int tid) {
     constexpr int E = 16, T = N / E, W = kCompute / T;
     const int c = tid % W, t = tid / W;
     const int col = in.tile * W + c;
@@ -158,34 +219,59 @@ __device__ __forceinline__ void ws_cols(float2 *stage, const StageInfo &in, cons
     for (int m = 0; m < E; m++) x[m] = sp[m * T * W];
     conj_line(x, cin);
     SyncCompute256{}();
-    LineFft<N, E, SyncCompute256>::run(x, t, ColSm<W>{stage, c}, tw);
+    ws_line<N>(x, t, ColSm<W>{stage, c}, tw, twc);
     finish_line(x, in.scale ? 1.0f / (float)N : 1.0f, cout);
-    if (active) store_line<N, E, T>(in.dst + col, (size_t)in.cols, x, t, in.flags & PF_SHIFT_ROWS);
+    // results back into the stage as the tensor-map box ([position][W]);
+    // columns past the image edge are clipped by the tensor store
+    (void)active;
+    SyncCompute256{}();
+    store_line<N, E, T>(stage + c, (size_t)W, x, t, in.flags & PF_SHIFT_ROWS);
 }
 
-__device__ __forceinline__ void ws_compute(float2 *stage, const StageInfo &in, const float2 *tw, int tid) {
+// Reload the shared-memory tables when the line length changes (every
+// compute thread sees the same items, so `cached_n` agrees across threads).
+__device__ __forceinline__ void tw_cache_for(int n, const float2 *tw, float4 *twc, int tid,
+                                             int &cached_n) {
+    if (n == cached_n || !tw_cached(n)) return;
+    SyncCompute256{}();  // every compute thread is done with the previous tables
+    switch (n) {
+    case 32: tw_fill_smem<32>(twc, tw, tid, kCompute); break;
+    case 64: tw_fill_smem<64>(twc, tw, tid, kCompute); break;
+    case 128: tw_fill_smem<128>(twc, tw, tid, kCompute); break;
+    case 256: tw_fill_smem<256>(twc, tw, tid, kCompute); break;
+    case 512: tw_fill_smem<512>(twc, tw, tid, kCompute); break;
+    case 1024: tw_fill_smem<1024>(twc, tw, tid, kCompute); break;
+    default: break;
+    }
+    SyncCompute256{}();
+    cached_n = n;
+}
+
+__device__ __forceinline__ void ws_compute(float2 *stage, const StageInfo &in, const float2 *tw,
+                                           float4 *twc, int tid, int &cached_n) {
+    tw_cache_for(in.along_rows ? in.cols : in.rows, tw, twc, tid, cached_n);
     if (in.along_rows) {
         switch (in.cols) {
-        case 16: ws_rows<16>(stage, in, tw, tid); break;
-        case 32: ws_rows<32>(stage, in, tw, tid); break;
-        case 64: ws_rows<64>(stage, in, tw, tid); break;
-        case 128: ws_rows<128>(stage, in, tw, tid); break;
-        case 256: ws_rows<256>(stage, in, tw, tid); break;
-        case 512: ws_rows<512>(stage, in, tw, tid); break;
-        case 1024: ws_rows<1024>(stage, in, tw, tid); break;
-        case 2048: ws_rows<2048>(stage, in, tw, tid); break;
-        case 4096: ws_rows<4096>(stage, in, tw, tid); break;
+        case 16: ws_rows<16>(stage, in, tw, twc, tid); break;
+        case 32: ws_rows<32>(stage, in, tw, twc, tid); break;
+        case 64: ws_rows<64>(stage, in, tw, twc, tid); break;
+        case 128: ws_rows<128>(stage, in, tw, twc, tid); break;
+        case 256: ws_rows<256>(stage, in, tw, twc, tid); break;
+        case 512: ws_rows<512>(stage, in, tw, twc, tid); break;
+        case 1024: ws_rows<1024>(stage, in, tw, twc, tid); break;
+        case 2048: ws_rows<2048>(stage, in, tw, twc, tid); break;
+        case 4096: ws_rows<4096>(stage, in, tw, twc, tid); break;
         default: break;
         }
     } else {
         switch (in.rows) {
-        case 16: ws_cols<16>(stage, in, tw, tid); break;
-        case 32: ws_cols<32>(stage, in, tw, tid); break;
-        case 64: ws_cols<64>(stage, in, tw, tid); break;
-        case 128: ws_cols<128>(stage, in, tw, tid); break;
-        case 256: ws_cols<256>(stage, in, tw, tid); break;
-        case 512: ws_cols<512>(stage, in, tw, tid); break;
-        case 1024: ws_cols<1024>(stage, in, tw, tid); break;
+        case 16: ws_cols<16>(stage, in, tw, twc, tid); break;
+        case 32: ws_cols<32>(stage, in, tw, twc, tid); break;
+        case 64: ws_cols<64>(stage, in, tw, twc, tid); break;
+        case 128: ws_cols<128>(stage, in, tw, twc, tid); break;
+        case 256: ws_cols<256>(stage, in, tw, twc, tid); break;
+        case 512: ws_cols<512>(stage, in, tw, twc, tid); break;
+        case 1024: ws_cols<1024>(stage, in, tw, twc, tid); break;
         default: break;
         }
     }
@@ -193,19 +279,21 @@ __device__ __forceinline__ void ws_compute(float2 *stage, const StageInfo &in, c
 
 }  // namespace
 
-template <int MINB>
+template <int MINB, int ST>
 __global__ void __launch_bounds__(kBlock, MINB) fft_batch_ws(BatchArgs a) {
     extern __shared__ __align__(128) unsigned char ws_raw[];
     // 128-byte aligned stage buffers, then the barriers and stage records
     unsigned char *base = reinterpret_cast<unsigned char *>(
         (reinterpret_cast<uintptr_t>(ws_raw) + 127) & ~uintptr_t(127));
     float2 *stages = reinterpret_cast<float2 *>(base);
-    WsShared &sh = *reinterpret_cast<WsShared *>(base + kStages * kStageBytes);
+    float4 *twc = reinterpret_cast<float4 *>(base + ST * kStageBytes);
+    WsShared<ST> &sh = *reinterpret_cast<WsShared<ST> *>(base + ST * kStageBytes +
+                                                 kTwCacheF4 * sizeof(float4));
 
     if (threadIdx.x == 0) {
-        for (int s = 0; s < kStages; s++) {
+        for (int s = 0; s < ST; s++) {
             mbar_init(&sh.full[s], 1);
-            mbar_init(&sh.stored[s], kCompute);
+            mbar_init(&sh.computed[s], kCompute);
         }
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
@@ -216,31 +304,58 @@ __global__ void __launch_bounds__(kBlock, MINB) fft_batch_ws(BatchArgs a) {
         if (threadIdx.x != kCompute) return;
         const int tile_px = kBatchTileElems;
         constexpr int kChunk = 4;  // items claimed per queue atomic
-        int issued = 0, published = 0;
+        int issued = 0, stored = 0, published = 0;
         bool failed = false;
-        // Publish the stored items [published, end) in order: one release
-        // fence, then one counter add per run of the same (image, pass).  A
-        // stage's record still describes its item until the item is
-        // published (the stage is refilled only after that).
+        // Publish the items [published, end) in order: one release fence,
+        // then one counter add per run of the same (image, pass), from the
+        // publication ring (at most kPubRing items are ever unpublished).
         auto publish_upto = [&](int end) {
             if (end <= published) return;
             asm volatile("fence.acq_rel.gpu;" ::: "memory");
             while (published < end) {
-                const int img = sh.info[published % kStages].image;
-                const int pas = sh.info[published % kStages].pass;
+                const int img = sh.pub_image[published % kPubRing];
+                const int pas = sh.pub_pass[published % kPubRing];
                 unsigned n = 0;
-                while (published < end && sh.info[published % kStages].image == img &&
-                       sh.info[published % kStages].pass == pas) {
+                while (published < end && sh.pub_image[published % kPubRing] == img &&
+                       sh.pub_pass[published % kPubRing] == pas) {
                     published++;
                     n++;
                 }
                 atomicAdd(a.done + img * kBatchMaxPasses + pas, n);
             }
         };
-        // publish every issued item whose tile the compute warps have stored
-        auto service = [&]() {
-            int end = published;
-            while (end < issued && mbar_test(&sh.stored[end % kStages], (end / kStages) & 1)) end++;
+        // the TMA store of item j, whose results are in stage j % ST
+        auto store_item = [&](int j) {
+            const StageInfo &inf = sh.info[j % ST];
+            const float2 *stage = stages + (size_t)(j % ST) * kStageElems;
+            if (inf.along_rows) {
+                const int n = inf.cols, lines = tile_px / n, row0 = inf.tile * lines;
+                const int nrows = min(lines, inf.rows - row0);
+                bulk_s2g(inf.dst + (size_t)row0 * n, stage, (unsigned)(nrows * n * sizeof(float2)));
+            } else {
+                const int n = inf.rows, w = tile_px / n, br = n < 256 ? n : 256;
+                const void *tmap = static_cast<const unsigned char *>(a.tmaps) + (size_t)inf.image * 128;
+                for (int b = 0; b < n / br; b++)
+                    tensor2d_s2g(tmap, inf.tile * w, b * br, stage + (size_t)b * br * w);
+            }
+            bulk_commit();
+        };
+        // store every item the compute warps have finished, in order (no wait)
+        auto store_ready = [&]() {
+            while (stored < issued &&
+                   mbar_test(&sh.computed[stored % ST], (stored / ST) & 1))
+                store_item(stored++);
+        };
+        // complete the stores of items [published, end) (end <= stored) and
+        // publish them; stores issued after item end-1 may stay in flight
+        auto complete_upto = [&](int end) {
+            if (end <= published) return;
+            const int newer = stored - end;
+            if (newer >= 2) bulk_wait<2>();
+            else if (newer == 1) bulk_wait<1>();
+            else bulk_wait<0>();
+            // the async-proxy writes are complete: order them before the release
+            asm volatile("fence.proxy.async.global;" ::: "memory");
             publish_upto(end);
         };
         const int chunk = a.claim_chunk < 1 ? 1 : (a.claim_chunk > kChunk ? kChunk : a.claim_chunk);
@@ -261,17 +376,28 @@ __global__ void __launch_bounds__(kBlock, MINB) fft_batch_ws(BatchArgs a) {
 #pragma unroll
             for (int q = 0; q <= kChunk; q++) {
                 if (q > cnt || (q == cnt && !done)) break;
-                const int s = issued % kStages;
-                // the stage's previous item must be stored (and is then published)
-                while (published <= issued - kStages) {
-                    if (!mbar_wait(&sh.stored[published % kStages], (published / kStages) & 1,
-                                   a.wait_limit_ns)) {
-                        failed = true;
-                        break;
+                const int s = issued % ST;
+                // the stage's previous item must be computed and its store
+                // must have read the stage before the stage is refilled
+                if (issued >= ST) {
+                    const int j = issued - ST;
+                    while (stored <= j) {
+                        if (!mbar_wait(&sh.computed[stored % ST], (stored / ST) & 1,
+                                       a.wait_limit_ns)) {
+                            failed = true;
+                            break;
+                        }
+                        store_ready();
                     }
-                    service();
+                    if (failed) break;
+                    const int newer = stored - j - 1;
+                    if (newer >= 2) bulk_wait_read<2>();
+                    else if (newer == 1) bulk_wait_read<1>();
+                    else bulk_wait_read<0>();
                 }
-                if (failed) break;
+                // publish what has surely landed; never let the ring overflow
+                if (issued - published >= kPubRing) complete_upto(issued - kPubRing + 1);
+                if (stored - 2 > published) complete_upto(stored - 2);
                 StageInfo &inf = sh.info[s];
                 if (q == cnt) {  // queue exhausted: tell the compute warps to stop
                     inf.valid = 0;
@@ -292,7 +418,8 @@ __global__ void __launch_bounds__(kBlock, MINB) fft_batch_ws(BatchArgs a) {
                     const unsigned *cnt_p = a.done + it.image * kBatchMaxPasses + it.pass - 1;
                     const unsigned long long t0 = gtimer();
                     while (ld_acquire_u32(cnt_p) < (unsigned)it.need) {
-                        service();
+                        store_ready();
+                        complete_upto(stored);
                         if ((long long)(gtimer() - t0) > a.wait_limit_ns) {
                             failed = true;
                             break;
@@ -314,6 +441,8 @@ __global__ void __launch_bounds__(kBlock, MINB) fft_batch_ws(BatchArgs a) {
                 inf.flags = ps.flags;
                 inf.scale = ps.scale;
                 inf.valid = 1;
+                sh.pub_image[issued % kPubRing] = it.image;
+                sh.pub_pass[issued % kPubRing] = it.pass;
                 float2 *stage = stages + (size_t)s * kStageElems;
                 if (ps.along_rows) {
                     const int n = im.cols, lines = tile_px / n;
@@ -334,77 +463,100 @@ __global__ void __launch_bounds__(kBlock, MINB) fft_batch_ws(BatchArgs a) {
                                      &sh.full[s]);
                 }
                 issued++;
-                service();
+                store_ready();
             }
             if (failed || done) break;
             if (!a.claim_ahead) claim = atomicAdd(a.head, (unsigned)chunk);
         }
         if (failed) {
             atomicExch(a.error, GLSFFT_ERROR_TIMEOUT);
-            // the compute warps finish what was issued, then stop here
-            const int s = issued % kStages;
+            // the compute warps finish what was issued, then stop here (the
+            // stage's previous item is let finish first, bounded)
+            if (issued >= ST && stored <= issued - ST)
+                mbar_wait(&sh.computed[(issued - ST) % ST],
+                          ((issued - ST) / ST) & 1, a.wait_limit_ns);
+            const int s = issued % ST;
             sh.info[s].valid = 0;
             mbar_arrive(&sh.full[s]);
         }
-        // publish what is left, and make sure no copy into this block's
-        // shared memory is still in flight when the block exits
-        while (published < issued) {
-            const int j = published;
-            if (mbar_wait(&sh.stored[j % kStages], (j / kStages) & 1, a.wait_limit_ns)) {
-                publish_upto(j + 1);
+        // store and publish what is left; make sure no copy into or out of
+        // this block's shared memory is in flight when the block exits
+        bool drain_ok = !failed;
+        while (stored < issued) {
+            const int j = stored;
+            if (drain_ok && mbar_wait(&sh.computed[j % ST], (j / ST) & 1, a.wait_limit_ns)) {
+                store_item(j);
             } else {
+                drain_ok = false;
                 atomicExch(a.error, GLSFFT_ERROR_TIMEOUT);
-                mbar_wait(&sh.full[j % kStages], (j / kStages) & 1, a.wait_limit_ns);
-                published++;
+                mbar_wait(&sh.full[j % ST], (j / ST) & 1, a.wait_limit_ns);
             }
+            stored++;
         }
+        bulk_wait<0>();
+        asm volatile("fence.proxy.async.global;" ::: "memory");
+        if (drain_ok) publish_upto(stored);
         return;
     }
 
     // ------------------------------------------------------------ compute
     const int tid = threadIdx.x;
+    int cached_n = -1;
     for (int k = 0;; k++) {
-        const int s = k % kStages;
-        if (!mbar_wait(&sh.full[s], (k / kStages) & 1, a.wait_limit_ns)) {
+        const int s = k % ST;
+        if (!mbar_wait(&sh.full[s], (k / ST) & 1, a.wait_limit_ns)) {
             if (tid == 0) atomicExch(a.error, GLSFFT_ERROR_TIMEOUT);
             break;
         }
         const StageInfo in = sh.info[s];
         if (!in.valid) break;
-        ws_compute(stages + (size_t)s * kStageElems, in, a.tw, tid);
-        // generic-proxy writes to the stage happen before the next TMA write
+        ws_compute(stages + (size_t)s * kStageElems, in, a.tw, twc, tid, cached_n);
+        // the generic-proxy writes of the results are ordered before the
+        // producer's TMA store (and the next TMA write into the stage)
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        mbar_arrive(&sh.stored[s]);
+        mbar_arrive(&sh.computed[s]);
     }
 }
 
-template <int MINB>
+// Variants: blocks per SM -> (min blocks, stages): 1 -> (1, 3), 2 -> (2, 3),
+// 3 -> (3, 2) (three blocks fit the SM's shared memory only with two stages).
+template <int MINB, int ST>
 static cudaError_t prepare_ws() {
     static cudaError_t once = cudaFuncSetAttribute(
-        fft_batch_ws<MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kWsSmem);
+        fft_batch_ws<MINB, ST>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ws_smem<ST>());
     return once;
 }
 
+template <int MINB, int ST>
+static int ws_per_sm() {
+    if (prepare_ws<MINB, ST>() != cudaSuccess) return 0;
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fft_batch_ws<MINB, ST>, kBlock,
+                                                      ws_smem<ST>()) != cudaSuccess)
+        return 0;
+    return per_sm;
+}
+
 cudaError_t launch_batch_ws(const BatchArgs &a, int grid, int blocks_per_sm, cudaStream_t s) {
-    cudaError_t e = blocks_per_sm >= 2 ? prepare_ws<2>() : prepare_ws<1>();
+    cudaError_t e = blocks_per_sm >= 3   ? prepare_ws<3, 2>()
+                    : blocks_per_sm == 2 ? prepare_ws<2, 3>()
+                                         : prepare_ws<1, 3>();
     if (e != cudaSuccess) return e;
-    if (blocks_per_sm >= 2) fft_batch_ws<2><<<grid, kBlock, kWsSmem, s>>>(a);
-    else fft_batch_ws<1><<<grid, kBlock, kWsSmem, s>>>(a);
+    if (blocks_per_sm >= 3) fft_batch_ws<3, 2><<<grid, kBlock, ws_smem<2>(), s>>>(a);
+    else if (blocks_per_sm == 2) fft_batch_ws<2, 3><<<grid, kBlock, ws_smem<3>(), s>>>(a);
+    else fft_batch_ws<1, 3><<<grid, kBlock, ws_smem<3>(), s>>>(a);
     return cudaGetLastError();
 }
 
 int batch_ws_grid(int device, int blocks_per_sm) {
-    cudaError_t e = blocks_per_sm >= 2 ? prepare_ws<2>() : prepare_ws<1>();
-    if (e != cudaSuccess) return 0;
-    int sms = 0, per_sm = 0;
+    int sms = 0;
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess)
         return 0;
-    e = blocks_per_sm >= 2
-            ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fft_batch_ws<2>, kBlock, kWsSmem)
-            : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fft_batch_ws<1>, kBlock, kWsSmem);
-    if (e != cudaSuccess) return 0;
+    int per_sm = blocks_per_sm >= 3 ? ws_per_sm<3, 2>() : blocks_per_sm == 2 ? ws_per_sm<2, 3>()
+                                                                             : ws_per_sm<1, 3>();
+    if (per_sm <= 0) return 0;
     if (per_sm > blocks_per_sm) per_sm = blocks_per_sm;
-    return sms * (per_sm > 0 ? per_sm : 1);
+    return sms * per_sm;
 }
 
 }  // namespace glsfft

@@ -27,8 +27,12 @@ namespace glsfft {
 // ------------------------------------------------------------ complex helpers
 __device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
 __device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+// Complex product with explicit fused multiply-adds: every kernel that
+// inlines it rounds the same way, whatever contraction the compiler would
+// choose, so the batch, pass and plain kernels give bit-identical lines.
 __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
-    return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+    return make_float2(__fmaf_rn(a.x, b.x, -__fmul_rn(a.y, b.y)),
+                       __fmaf_rn(a.x, b.y, __fmul_rn(a.y, b.x)));
 }
 __device__ __forceinline__ float2 cconj(float2 a) { return make_float2(a.x, -a.y); }
 __device__ __forceinline__ float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
@@ -75,7 +79,7 @@ __device__ __forceinline__ float2 wmul(float2 v) {
                           : (k16 == 5 || k16 == 11) ? -S1 : -C1;
         constexpr float s = (k16 == 1 || k16 == 7) ? -S1 : (k16 == 3 || k16 == 5) ? -C1
                           : (k16 == 9 || k16 == 15) ? S1 : C1;
-        return make_float2(v.x * c - v.y * s, v.x * s + v.y * c);
+        return make_float2(__fmaf_rn(v.x, c, -__fmul_rn(v.y, s)), __fmaf_rn(v.x, s, __fmul_rn(v.y, c)));
     }
 }
 
@@ -153,6 +157,83 @@ struct SyncCompute256 {
     }
 };
 
+// ------------------------------------------------------ twiddle sources
+// Row k of the table of a pass with radix R and span L = Ns*R: w^(R/2) in
+// w[0] (R > 2) and w^1..w^(R/2-1) in w[1..], w = e^{-2 pi i k / L}; for
+// R = 2, w[0] = w^1.  From the global tables (tw_offset layout):
+template <int N, int MB, int P_, int R, int L>
+__device__ __forceinline__ void tw_row(const float2 *__restrict__ tw, int k, float2 (&w)[R / 2]) {
+    const float2 *wt = tw + tw_offset(R, L) + k * R;
+    if constexpr (R == 2) {
+        w[0] = __ldg(wt);
+    } else {
+        const float4 *w4 = reinterpret_cast<const float4 *>(wt);
+#pragma unroll
+        for (int h = 0; h < R / 4; h++) {
+            const float4 q = __ldg(w4 + h);
+            w[2 * h] = make_float2(q.x, q.y);
+            w[2 * h + 1] = make_float2(q.z, q.w);
+        }
+    }
+}
+
+// A line's tables for passes 1..P-1 copied into shared memory.  Pass p's
+// table (L_p / R_p rows of R_p / 4 float4 vectors) is stored vector-major,
+// [vector h][row k], so the consecutive butterflies of a warp read
+// consecutive 16-byte words.  Needs R_p >= 4 for every p >= 1.
+__host__ __device__ constexpr int tw_smem_offset4(int n, int p, int mb) {
+    return p <= 1 ? 0
+                  : tw_smem_offset4(n, p - 1, mb) + pass_span(n, p - 1, mb) * pass_radix(n, p - 1, mb) / 4;
+}
+__host__ __device__ constexpr int tw_smem_float4(int n, int mb = 4) {
+    return num_passes(n, mb) <= 1 ? 0 : tw_smem_offset4(n, num_passes(n, mb), mb);
+}
+__host__ __device__ constexpr bool tw_smem_ok_from(int n, int p, int mb) {
+    return p >= num_passes(n, mb) ? true : (pass_radix(n, p, mb) >= 4 && tw_smem_ok_from(n, p + 1, mb));
+}
+__host__ __device__ constexpr bool tw_smem_ok(int n, int mb = 4) { return tw_smem_ok_from(n, 1, mb); }
+
+template <int N, int MB = 4>
+struct SmemTw {
+    const float4 *base;  // shared memory, tw_smem_float4(N, MB) vectors
+};
+
+template <int N, int MB, int P_, int R, int L>
+__device__ __forceinline__ void tw_row(const SmemTw<N, MB> &tw, int k, float2 (&w)[R / 2]) {
+    static_assert(R >= 4, "shared-memory twiddles need radix >= 4");
+    constexpr int rows = L / R;
+    const float4 *w4 = tw.base + tw_smem_offset4(N, P_, MB) + k;
+#pragma unroll
+    for (int h = 0; h < R / 4; h++) {
+        const float4 q = w4[h * rows];
+        w[2 * h] = make_float2(q.x, q.y);
+        w[2 * h + 1] = make_float2(q.z, q.w);
+    }
+}
+
+// Copy a line's tables from the global tables into `dst` (shared memory);
+// threads tid = 0..nthreads-1 share the work.
+template <int N, int MB, int p>
+__device__ __forceinline__ void tw_fill_pass(float4 *dst, const float2 *__restrict__ tw, int tid,
+                                             int nthreads) {
+    if constexpr (p < num_passes(N, MB)) {
+        constexpr int R = pass_radix(N, p, MB), L = pass_span(N, p, MB) * R, rows = L / R;
+        const float4 *src = reinterpret_cast<const float4 *>(tw + tw_offset(R, L));
+        float4 *d = dst + tw_smem_offset4(N, p, MB);
+        for (int i = tid; i < rows * (R / 4); i += nthreads) {
+            const int k = i % rows, h = i / rows;
+            d[h * rows + k] = __ldg(src + k * (R / 2) + h);
+        }
+        tw_fill_pass<N, MB, p + 1>(dst, tw, tid, nthreads);
+    }
+}
+template <int N, int MB = 4>
+__device__ __forceinline__ void tw_fill_smem(float4 *dst, const float2 *__restrict__ tw, int tid,
+                                             int nthreads) {
+    static_assert(tw_smem_ok(N, MB), "a pass with radix 2 has no shared-memory table");
+    tw_fill_pass<N, MB, 1>(dst, tw, tid, nthreads);
+}
+
 // Shared-memory accessors map a line position to a padded slot: the linear
 // index i (position * KW + column) gets one pad per 16, slot = i + i/16.
 // Strided<Sm, DELTA, COUNT> tells whether COUNT accesses DELTA positions
@@ -178,15 +259,15 @@ struct LineFft {
     static constexpr int T = (N >= E) ? N / E : 1;
     static constexpr int P = num_passes(N, MB);
 
-    template <class Sm>
-    __device__ __forceinline__ static void run(float2 (&x)[E], int t, Sm sm,
-                                               const float2 *__restrict__ tw) {
+    // Tw: const float2 * (the global tables) or SmemTw<N, MB> (a copy in
+    // shared memory)
+    template <class Sm, class Tw>
+    __device__ __forceinline__ static void run(float2 (&x)[E], int t, Sm sm, Tw tw) {
         pass<0>(x, t, sm, tw);
     }
 
-    template <int p, class Sm>
-    __device__ __forceinline__ static void pass(float2 (&x)[E], int t, Sm sm,
-                                                const float2 *__restrict__ tw) {
+    template <int p, class Sm, class Tw>
+    __device__ __forceinline__ static void pass(float2 (&x)[E], int t, Sm sm, Tw tw) {
         if constexpr (p < P) {
             [[maybe_unused]] const Sync sync{};
             constexpr int R = pass_radix(N, p, MB);
@@ -206,18 +287,11 @@ struct LineFft {
                     // the twiddle loads (entry R/2 is stored in slot 0, whose
                     // value w^0 = 1 is never needed)
                     const int k = j & (Ns - 1);
-                    const float2 *wt = tw + tw_offset(R, Ns * R) + k * R;
+                    float2 w[R / 2];
+                    tw_row<N, MB, p, R, Ns * R>(tw, k, w);
                     if constexpr (R == 2) {
-                        v[1] = cmul(v[1], __ldg(wt));
+                        v[1] = cmul(v[1], w[0]);
                     } else {
-                        float2 w[R / 2];
-                        const float4 *w4 = reinterpret_cast<const float4 *>(wt);
-#pragma unroll
-                        for (int h = 0; h < R / 4; h++) {
-                            const float4 q = __ldg(w4 + h);
-                            w[2 * h] = make_float2(q.x, q.y);
-                            w[2 * h + 1] = make_float2(q.z, q.w);
-                        }
                         const float2 wh = w[0];  // w^(R/2)
 #pragma unroll
                         for (int r = 1; r < R / 2; r++) {

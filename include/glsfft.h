@@ -194,14 +194,17 @@ GLSFFT_API int glsfft_batch_execute(glsfft_batch plan, void *stream);
 
 /*
  * Persistent-kernel schedule of a plan (re-captures its graph):
- * 0 = every thread loads its own operands (2 blocks/SM);
+ * 0 = every thread loads and stores its own operands (2 blocks/SM);
  * 1 = warp-specialised: a producer warp stages tiles with TMA into a 3-stage
- *     shared-memory ring for 8 compute warps (1 block/SM);
- * 2 = the same at 2 blocks/SM (registers capped at 96; the default).
+ *     shared-memory ring for 8 compute warps and writes the results back
+ *     with TMA stores (1 block/SM);
+ * 2 = the same at 2 blocks/SM (the default);
+ * 3 = the same at 3 blocks/SM with a 2-stage ring.
  */
 #define GLSFFT_BATCH_PLAIN 0
 #define GLSFFT_BATCH_TMA_WS1 1
 #define GLSFFT_BATCH_TMA_WS2 2
+#define GLSFFT_BATCH_TMA_WS3 3
 GLSFFT_API int glsfft_batch_set_variant(glsfft_batch plan, int variant);
 
 /*
@@ -240,7 +243,7 @@ GLSFFT_API int glsfft_batch_get_schedule(glsfft_batch plan, int *schedule4);
  * that get their own pass launches have their per-size pass schedules tuned
  * (glsfft_autotune_fft2d).  Then every persistent-kernel schedule -- variant
  * (GLSFFT_BATCH_*) x item-order lag (1, 2, 4, 8 resident grids) x claim
- * chunk (1, 2, 4) x claim-ahead (0, 1) -- is timed, `reps` graph launches
+ * chunk (1, 2, 4) x claim-ahead (0, 1), 76 in all -- is timed, `reps` graph launches
  * each (median, CUDA events on `stream`), on a shadow plan of the same
  * shapes, flags, alignments and aliasing over scratch buffers, so the
  * plan's own images are never read or written.  The fastest is applied to

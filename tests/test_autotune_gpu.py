@@ -142,8 +142,8 @@ def test_batch_autotune_leaves_images_untouched_and_caches(tctx, torch_cuda, ora
         assert np.array_equal(d_in[i].cpu().numpy(), before_in[i])
         assert not d_out[i].cpu().numpy().any()
     assert not res["from_cache"]
-    assert res["candidates"] == 24 + 24 + 4  # WS2, WS1: 4 lags x 3 chunks x 2; plain: 4 lags
-    assert res["variant"] in (0, 1, 2) and 1 <= res["claim_chunk"] <= 4
+    assert res["candidates"] == 3 * 24 + 4  # WS1-3: 4 lags x 3 chunks x 2; plain: 4 lags
+    assert res["variant"] in (0, 1, 2, 3) and 1 <= res["claim_chunk"] <= 4
     assert b.schedule()["variant"] == res["variant"]
     assert b.schedule()["lag_items"] == res["lag_items"]
     assert 0 < res["ms"] <= res["ms_default"] * 1.0001

@@ -41,7 +41,7 @@ def _single(ctx, torch, x, flags):
     return y
 
 
-@pytest.mark.parametrize("variant", [0, 1, 2])
+@pytest.mark.parametrize("variant", [0, 1, 2, 3])
 @pytest.mark.parametrize("flags", [(0,), (0, INV | SCALE), (SHIFT,), (INV, SCALE | SHIFT)])
 def test_uneven_batch_bit_identical_to_single_path(ctx, torch_cuda, flags, variant):
     torch = torch_cuda
@@ -76,7 +76,7 @@ def test_config3_batch_vs_oracle_and_replay(ctx, torch_cuda, oracle):
     b.close()
 
 
-@pytest.mark.parametrize("variant", [0, 1, 2])
+@pytest.mark.parametrize("variant", [0, 1, 2, 3])
 def test_inplace_round_trip_batch(ctx, torch_cuda, oracle, variant):
     torch = torch_cuda
     shapes = [(1024, 1024)] * 6 + [(256, 512)] * 5
@@ -87,7 +87,7 @@ def test_inplace_round_trip_batch(ctx, torch_cuda, oracle, variant):
     b.close()
 
 
-@pytest.mark.parametrize("variant", [0, 1, 2])
+@pytest.mark.parametrize("variant", [0, 1, 2, 3])
 def test_injected_stall_times_out_and_context_survives(ctx, torch_cuda, oracle, variant):
     torch = torch_cuda
     shapes = [(256, 256)] * 4
