@@ -51,6 +51,9 @@ def parse():
                         "the plan keeps its default schedule")
     p.add_argument("--no-autotune", action="store_true",
                    help="keep the batch plans' default schedules")
+    p.add_argument("--schedule", default=None,
+                   help="variant,claim_chunk,claim_ahead,lag_grids for the headline plan "
+                        "instead of autotuning it (e.g. 3,1,1,8)")
     p.add_argument("--no-uneven", action="store_true",
                    help="skip the 512-image uneven-size batch section")
     return p.parse_args()
@@ -460,7 +463,12 @@ def run_own(args) -> None:
     # warp-specialised launch per step (graph: a counter memset + the kernel)
     plan = g.Batch(ctx, ptr_in, ptr_out, [(ROWS, COLS)] * B, (0, INV | SCALE))
     tune = None
-    if not (args.no_autotune or args.profile_only):
+    if args.schedule:
+        v, c, ah, lg = (int(x) for x in args.schedule.split(","))
+        plan.set_variant(v)
+        plan.set_schedule(c, ah, lg * plan.info()["grid"])
+        tune = {"fixed": plan.schedule()}
+    elif not (args.no_autotune or args.profile_only):
         tt = time.perf_counter()
         tune = plan.autotune(None, reps=5, stream=s)
         tune["seconds"] = round(time.perf_counter() - tt, 3)

@@ -61,6 +61,9 @@ _SIGNATURES = {
                                 ctypes.POINTER(_ip)]),
     "glsfft_batch_inject_stall": (_ip, [_vp, ctypes.c_longlong]),
     "glsfft_batch_get_schedule": (_ip, [_vp, ctypes.POINTER(_ip)]),
+    "glsfft_batch_tuning": (_ip, [_vp, _ip, ctypes.POINTER(_ip), _dp, ctypes.POINTER(_ip)]),
+    "glsfft_batch_set_stats": (_ip, [_vp, _ip]),
+    "glsfft_batch_get_stats": (_ip, [_vp, _vp, _dp]),
     "glsfft_batch_autotune": (_ip, [_vp, ctypes.c_char_p, _ip, _vp, ctypes.POINTER(_ip), _dp]),
     "glsfft_schedule_available": (_ip, [_ip, _ip, _ip]),
     "glsfft_set_fft_schedule": (_ip, [_vp, _ip, _ip, _ip, _ip]),
@@ -238,7 +241,7 @@ class Batch:
     def set_variant(self, variant: int) -> None:
         check(lib().glsfft_batch_set_variant(self.handle, int(variant)), "batch_set_variant")
 
-    def set_schedule(self, claim_chunk: int = 1, claim_ahead: bool = False,
+    def set_schedule(self, claim_chunk: int = 1, claim_ahead: int = 0,
                      lag_items: int = 0) -> None:
         check(lib().glsfft_batch_set_schedule(self.handle, int(claim_chunk), int(claim_ahead),
                                               int(lag_items)), "batch_set_schedule")
@@ -260,6 +263,27 @@ class Batch:
         check(lib().glsfft_batch_get_schedule(self.handle, out), "batch_get_schedule")
         return {"variant": out[0], "claim_chunk": out[1], "claim_ahead": out[2],
                 "lag_items": out[3]}
+
+    def tuning(self) -> list[dict]:
+        """Candidates of the last timed autotune: schedule and median ms."""
+        n = _ip()
+        check(lib().glsfft_batch_tuning(self.handle, 0, None, None, ctypes.byref(n)), "tuning")
+        sch = (_ip * (4 * n.value))()
+        ms = (ctypes.c_double * n.value)()
+        check(lib().glsfft_batch_tuning(self.handle, n.value, sch, ms, ctypes.byref(n)), "tuning")
+        return [{"variant": sch[4 * i], "claim_chunk": sch[4 * i + 1],
+                 "claim_ahead": sch[4 * i + 2], "lag_grids": sch[4 * i + 3], "ms": ms[i]}
+                for i in range(n.value)]
+
+    def set_stats(self, on: bool) -> None:
+        check(lib().glsfft_batch_set_stats(self.handle, int(on)), "batch_set_stats")
+
+    def stats(self, stream: int = 0) -> dict:
+        out = (ctypes.c_double * 8)()
+        check(lib().glsfft_batch_get_stats(self.handle, stream, out), "batch_get_stats")
+        keys = ["dep_wait_ns", "refill_wait_ns", "publish_wait_ns", "producer_ns",
+                "full_wait_ns", "compute_ns", "items", "blocks"]
+        return dict(zip(keys, list(out)))
 
     def autotune(self, cache_path: str | None = None, reps: int = 5, stream: int = 0) -> dict:
         res = (_ip * 6)()

@@ -31,7 +31,7 @@ struct glsfft_batch_s {
     int n_images = 0;      // images in the persistent launch
     int n_items = 0;
     int grid = 0;
-    int variant = BATCH_TMA_WS2;   // the fastest schedule measured on GB300
+    int variant = BATCH_TMA_WS3;   // the fastest variant measured on GB300
     void *d_mem = nullptr;  // tensor maps | images | passes | items | head, done, error
     BatchArgs args{};
     std::vector<BatchImage> images;
@@ -48,15 +48,21 @@ struct glsfft_batch_s {
     long long wait_limit_ns = 2000000000LL;
     size_t o_items = 0;
     int lag_items = 0;  // the item order's lag (order_items)
+    unsigned long long *d_stats = nullptr;  // kBatchStats timing sums, when enabled
+    struct Cand {
+        int v, c, a, lg;
+        double ms;
+    };
+    std::vector<Cand> tuned;  // the last autotuning's candidates
 };
 
 namespace {
 
-// Default schedule: two warp-specialised blocks per SM, items claimed two at
-// a time, an image's next pass listed four resident grids after its previous
-// one (glsfft_batch_set_schedule / the autotuner can change all three).
+// Default schedule: three warp-specialised blocks per SM, items claimed two
+// at a time, an image's next pass listed eight resident grids after its
+// previous one (glsfft_batch_set_schedule / the autotuner can change all).
 constexpr int kDefaultClaimChunk = 2;
-constexpr int kDefaultLagGrids = 4;
+constexpr int kDefaultLagGrids = 8;
 
 int row_tiles_of(int rows, int cols) {
     const int lines = kBatchTileElems / cols;
@@ -338,7 +344,7 @@ int glsfft_batch_set_schedule(glsfft_batch plan, int claim_chunk, int claim_ahea
     DeviceGuard g(plan->device);
     if (!g.ok()) return GLSFFT_ERROR_CUDA;
     plan->args.claim_chunk = claim_chunk;
-    plan->args.claim_ahead = claim_ahead ? 1 : 0;
+    plan->args.claim_ahead = claim_ahead < 0 ? 0 : (claim_ahead > 2 ? 2 : claim_ahead);
     if (plan->n_images > 0 && lag_blocks > 0) {
         std::vector<BatchItem> items = order_items(plan->images, plan->passes, lag_blocks);
         cudaError_t e = cudaMemcpy(static_cast<char *>(plan->d_mem) + plan->o_items, items.data(),
@@ -466,7 +472,7 @@ int glsfft_batch_autotune(glsfft_batch plan, const char *cache_path, int reps, v
         const int v = std::atoi(hit["variant"].c_str()), c = std::atoi(hit["claim_chunk"].c_str()),
                   a = std::atoi(hit["claim_ahead"].c_str()),
                   lg = std::atoi(hit["lag_grids"].c_str());
-        if (v >= BATCH_PLAIN && v <= BATCH_TMA_WS3 && c >= 1 && c <= 4 && (a == 0 || a == 1) &&
+        if (v >= BATCH_PLAIN && v <= BATCH_TMA_WS3 && c >= 1 && c <= 4 && a >= 0 && a <= 2 &&
             lg >= 1) {
             st = apply(v, c, a, lg);
             if (st) return st;
@@ -536,10 +542,7 @@ int glsfft_batch_autotune(glsfft_batch plan, const char *cache_path, int reps, v
 
     // 4. every schedule: variant x item-order lag (resident grids) x claim
     //    chunk x claim-ahead (the plain variant has no claim knobs)
-    struct Cand {
-        int v, c, a, lg;
-        double ms;
-    };
+    using Cand = glsfft_batch_s::Cand;
     std::vector<Cand> cands;
     const int variants[4] = {BATCH_TMA_WS2, BATCH_TMA_WS3, BATCH_TMA_WS1, BATCH_PLAIN};
     const int lags[4] = {1, 2, 4, 8};
@@ -547,8 +550,9 @@ int glsfft_batch_autotune(glsfft_batch plan, const char *cache_path, int reps, v
         for (int lg : lags) {
             for (int c = 1; c <= 4 && !st; c *= 2) {
                 if (v == BATCH_PLAIN && c != kDefaultClaimChunk) continue;
-                for (int a = 0; a <= 1 && !st; a++) {
+                for (int a = 0; a <= 2 && !st; a++) {
                     if (v == BATCH_PLAIN && a) continue;
+                    if (a == 2 && c != 1) continue;  // deep prefetch claims one item at a time
                     st = glsfft_batch_set_variant(shadow, v);
                     if (!st) st = glsfft_batch_set_schedule(shadow, c, a, lg * shadow->grid);
                     double m = 0.0;
@@ -571,12 +575,13 @@ int glsfft_batch_autotune(glsfft_batch plan, const char *cache_path, int reps, v
     cudaGetLastError();
     if (st) return st;
     if (cands.empty()) return GLSFFT_ERROR_TIMEOUT;
+    plan->tuned = cands;
 
     // 5. the fastest, unless the default schedule is within the keep margin
     const Cand *best = &cands[0], *def = nullptr;
     for (const auto &c : cands) {
         if (c.ms < best->ms) best = &c;
-        if (c.v == BATCH_TMA_WS2 && c.c == kDefaultClaimChunk && c.a == 0 &&
+        if (c.v == BATCH_TMA_WS3 && c.c == kDefaultClaimChunk && c.a == 0 &&
             c.lg == kDefaultLagGrids)
             def = &c;
     }
@@ -608,9 +613,64 @@ int glsfft_batch_autotune(glsfft_batch plan, const char *cache_path, int reps, v
     return st;
 }
 
+int glsfft_batch_set_stats(glsfft_batch plan, int on) {
+    if (!plan) return GLSFFT_ERROR_INVALID_VALUE;
+    DeviceGuard g(plan->device);
+    if (!g.ok()) return GLSFFT_ERROR_CUDA;
+    if (on && !plan->d_stats) {
+        void *p = nullptr;
+        if (cudaMalloc(&p, sizeof(unsigned long long) * kBatchStats) != cudaSuccess) {
+            cudaGetLastError();
+            return GLSFFT_ERROR_OUT_OF_MEMORY;
+        }
+        cudaError_t e = cudaMemset(p, 0, sizeof(unsigned long long) * kBatchStats);
+        if (e != cudaSuccess) {
+            cudaFree(p);
+            return cuda_status(e);
+        }
+        plan->d_stats = static_cast<unsigned long long *>(p);
+    }
+    plan->args.stats = on ? plan->d_stats : nullptr;
+    return capture(plan);
+}
+
+int glsfft_batch_get_stats(glsfft_batch plan, void *stream, double *out) {
+    if (!plan || !out) return GLSFFT_ERROR_INVALID_VALUE;
+    for (int i = 0; i < kBatchStats; i++) out[i] = 0.0;
+    if (!plan->d_stats) return GLSFFT_SUCCESS;
+    DeviceGuard g(plan->device);
+    if (!g.ok()) return GLSFFT_ERROR_CUDA;
+    unsigned long long h[kBatchStats];
+    cudaError_t e = cudaMemcpyAsync(h, plan->d_stats, sizeof h, cudaMemcpyDeviceToHost,
+                                    (cudaStream_t)stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize((cudaStream_t)stream);
+    if (e == cudaSuccess)
+        e = cudaMemsetAsync(plan->d_stats, 0, sizeof h, (cudaStream_t)stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize((cudaStream_t)stream);
+    if (e != cudaSuccess) return cuda_status(e);
+    for (int i = 0; i < kBatchStats; i++) out[i] = (double)h[i];
+    return GLSFFT_SUCCESS;
+}
+
+int glsfft_batch_tuning(glsfft_batch plan, int max, int *sched4, double *ms, int *count) {
+    if (!plan || !count || max < 0 || (max > 0 && (!sched4 || !ms)))
+        return GLSFFT_ERROR_INVALID_VALUE;
+    *count = (int)plan->tuned.size();
+    for (int i = 0; i < max && i < (int)plan->tuned.size(); i++) {
+        const auto &c = plan->tuned[i];
+        sched4[4 * i] = c.v;
+        sched4[4 * i + 1] = c.c;
+        sched4[4 * i + 2] = c.a;
+        sched4[4 * i + 3] = c.lg;
+        ms[i] = c.ms;
+    }
+    return GLSFFT_SUCCESS;
+}
+
 int glsfft_batch_destroy(glsfft_batch plan) {
     if (!plan) return GLSFFT_ERROR_INVALID_VALUE;
     DeviceGuard g(plan->device);
+    if (plan->d_stats) cudaFree(plan->d_stats);
     if (plan->exec) cudaGraphExecDestroy(plan->exec);
     if (plan->graph) cudaGraphDestroy(plan->graph);
     if (plan->d_mem) cudaFree(plan->d_mem);

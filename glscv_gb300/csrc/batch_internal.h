@@ -51,13 +51,31 @@ struct BatchArgs {
     const void *tmaps;     // warp-specialised kernel: one 128-B CUtensorMap per image (dst)
     int claim_chunk;       // warp-specialised kernel: items claimed per queue atomic (1..4)
     int claim_ahead;       // 1: claim the next chunk before working on the current one
+    unsigned long long *stats;  // warp-specialised kernel: kBatchStats timing sums, or null
 };
 
-// Persistent kernel variants: plain (every thread loads its operands) and
-// warp-specialised (a producer warp stages tiles with TMA into a 3-stage
-// shared-memory ring; eight compute warps run the FFT and store).
-// The warp-specialised kernel comes compiled for 1 and for 2 blocks per SM
-// (at 2, nine warps per block cap registers at 96 and the FFT spills a little).
+// Timing sums (nanoseconds, %globaltimer) a warp-specialised launch adds
+// when BatchArgs::stats is set: per block, producer time in dependency
+// waits, in waits for a stage to be free (compute done + store read), in
+// store-completion waits before publishing, and its whole run; compute
+// warp 0's waits for staged tiles and its whole run; items issued.
+enum {
+    BS_DEP_WAIT = 0,
+    BS_REFILL_WAIT,
+    BS_PUBLISH_WAIT,
+    BS_PRODUCER_TOTAL,
+    BS_FULL_WAIT,
+    BS_COMPUTE_TOTAL,
+    BS_ITEMS,
+    BS_BLOCKS,
+    kBatchStats
+};
+
+// Persistent kernel variants: plain (every thread loads and stores its
+// operands) and warp-specialised (a producer warp stages tiles with TMA into
+// a shared-memory ring, eight compute warps run the FFT and leave the results
+// in the stage, the producer stores them with TMA): 1 or 2 blocks per SM
+// with 3 stages, or 3 blocks per SM with 2 stages.
 enum { BATCH_PLAIN = 0, BATCH_TMA_WS1 = 1, BATCH_TMA_WS2 = 2, BATCH_TMA_WS3 = 3 };
 
 cudaError_t launch_batch_persistent(const BatchArgs &a, int grid, cudaStream_t s);

@@ -57,6 +57,7 @@ struct WsShared {
     StageInfo info[ST];
     int pub_image[kPubRing];
     int pub_pass[kPubRing];
+    unsigned long long st[6];  // timing sums when BatchArgs::stats is set (BS_* order)
 };
 
 // Shared-memory copy of the twiddle tables of the current line length, for
@@ -121,6 +122,16 @@ __device__ bool mbar_wait(unsigned long long *b, unsigned parity, long long limi
         if ((long long)(gtimer() - t0) > limit_ns) return false;
     }
     return false;
+}
+__device__ __forceinline__ unsigned ld_relaxed_u32(const unsigned *p) {
+    unsigned v;
+    asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ int ld_relaxed_s32(const int *p) {
+    int v;
+    asm volatile("ld.relaxed.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
 }
 __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned *p) {
     unsigned v;
@@ -291,6 +302,7 @@ __global__ void __launch_bounds__(kBlock, MINB) fft_batch_ws(BatchArgs a) {
                                                  kTwCacheF4 * sizeof(float4));
 
     if (threadIdx.x == 0) {
+        for (int i = 0; i < 6; i++) sh.st[i] = 0;
         for (int s = 0; s < ST; s++) {
             mbar_init(&sh.full[s], 1);
             mbar_init(&sh.computed[s], kCompute);
@@ -303,6 +315,8 @@ __global__ void __launch_bounds__(kBlock, MINB) fft_batch_ws(BatchArgs a) {
         // ------------------------------------------------------ producer
         if (threadIdx.x != kCompute) return;
         const int tile_px = kBatchTileElems;
+        // optional timing sums (BatchArgs::stats), kept in shared memory
+        if (a.stats) sh.st[BS_PRODUCER_TOTAL] = gtimer();
         constexpr int kChunk = 4;  // items claimed per queue atomic
         int issued = 0, stored = 0, published = 0;
         bool failed = false;
@@ -350,123 +364,196 @@ __global__ void __launch_bounds__(kBlock, MINB) fft_batch_ws(BatchArgs a) {
         // publish them; stores issued after item end-1 may stay in flight
         auto complete_upto = [&](int end) {
             if (end <= published) return;
+            const unsigned long long tw0 = a.stats ? gtimer() : 0;
             const int newer = stored - end;
             if (newer >= 2) bulk_wait<2>();
             else if (newer == 1) bulk_wait<1>();
             else bulk_wait<0>();
             // the async-proxy writes are complete: order them before the release
             asm volatile("fence.proxy.async.global;" ::: "memory");
+            if (a.stats) sh.st[BS_PUBLISH_WAIT] += gtimer() - tw0;
             publish_upto(end);
         };
-        const int chunk = a.claim_chunk < 1 ? 1 : (a.claim_chunk > kChunk ? kChunk : a.claim_chunk);
-        unsigned claim = atomicAdd(a.head, (unsigned)chunk);
         int cur_img = -1, cur_pass = -1, cur_need = -1;
         bool dep_ok = false;
         BatchImage im{};
         BatchPass ps{};
-        for (;;) {
-            const int base = (int)claim;
-            const bool done = base >= a.n_items || *(volatile int *)a.error;
-            if (!done && a.claim_ahead) claim = atomicAdd(a.head, (unsigned)chunk);  // in flight
-            const int cnt = done ? 0 : min(chunk, a.n_items - base);
-            BatchItem its[kChunk];
-#pragma unroll
-            for (int q = 0; q < kChunk; q++)
-                if (q < cnt) its[q] = a.items[base + q];
-#pragma unroll
-            for (int q = 0; q <= kChunk; q++) {
-                if (q > cnt || (q == cnt && !done)) break;
-                const int s = issued % ST;
-                // the stage's previous item must be computed and its store
-                // must have read the stage before the stage is refilled
-                if (issued >= ST) {
-                    const int j = issued - ST;
-                    while (stored <= j) {
-                        if (!mbar_wait(&sh.computed[stored % ST], (stored / ST) & 1,
-                                       a.wait_limit_ns)) {
-                            failed = true;
-                            break;
-                        }
-                        store_ready();
-                    }
-                    if (failed) break;
-                    const int newer = stored - j - 1;
-                    if (newer >= 2) bulk_wait_read<2>();
-                    else if (newer == 1) bulk_wait_read<1>();
-                    else bulk_wait_read<0>();
-                }
-                // publish what has surely landed; never let the ring overflow
-                if (issued - published >= kPubRing) complete_upto(issued - kPubRing + 1);
-                if (stored - 2 > published) complete_upto(stored - 2);
-                StageInfo &inf = sh.info[s];
-                if (q == cnt) {  // queue exhausted: tell the compute warps to stop
-                    inf.valid = 0;
-                    mbar_arrive(&sh.full[s]);
-                    break;
-                }
-                const BatchItem it = its[q];
+        // Issue one item into the next stage, or the stop record (itp null).
+        // `pre` is the item's image record when the caller fetched it ahead;
+        // `spec` a relaxed look at its dependency counter (UINT_MAX: none).
+        // The item's records and dependency come first, so their latency
+        // overlaps the compute warps' work on the stages in flight; then
+        // the stage is waited for.  Returns false when a wait expired.
+        auto issue_item = [&](const BatchItem *itp, const BatchImage *pre, unsigned spec) -> bool {
+            const int s = issued % ST;
+            if (itp) {
+                const BatchItem &it = *itp;
                 if (it.image != cur_img || it.pass != cur_pass || it.need != cur_need) {
-                    if (it.image != cur_img) im = a.images[it.image];
+                    if (it.image != cur_img) im = pre ? *pre : a.images[it.image];
                     if (it.pass != cur_pass) ps = a.passes[it.pass];
                     cur_img = it.image;
                     cur_pass = it.pass;
                     cur_need = it.need;
                     dep_ok = it.pass == 0;
                 }
+                if (!dep_ok && spec != 0xffffffffu && spec >= (unsigned)it.need) {
+                    // the relaxed read saw every tile published: make it an acquire
+                    asm volatile("fence.acq_rel.gpu;" ::: "memory");
+                    asm volatile("fence.proxy.async.global;" ::: "memory");
+                    dep_ok = true;
+                }
                 if (!dep_ok) {
                     // every tile of this image's previous pass must be published
                     const unsigned *cnt_p = a.done + it.image * kBatchMaxPasses + it.pass - 1;
                     const unsigned long long t0 = gtimer();
+                    const unsigned long long pub0 = a.stats ? sh.st[BS_PUBLISH_WAIT] : 0;
+                    bool ok = true;
                     while (ld_acquire_u32(cnt_p) < (unsigned)it.need) {
                         store_ready();
                         complete_upto(stored);
                         if ((long long)(gtimer() - t0) > a.wait_limit_ns) {
-                            failed = true;
+                            ok = false;
                             break;
                         }
                         __nanosleep(128);
                     }
-                    if (failed) break;
+                    if (a.stats)
+                        sh.st[BS_DEP_WAIT] += gtimer() - t0 - (sh.st[BS_PUBLISH_WAIT] - pub0);
+                    if (!ok) return false;
                     // order the acquire before the async-proxy (TMA) reads
                     asm volatile("fence.proxy.async.global;" ::: "memory");
                     dep_ok = true;
                 }
-                inf.dst = im.dst;
-                inf.rows = im.rows;
-                inf.cols = im.cols;
-                inf.tile = it.tile;
-                inf.image = it.image;
-                inf.pass = it.pass;
-                inf.along_rows = ps.along_rows;
-                inf.flags = ps.flags;
-                inf.scale = ps.scale;
-                inf.valid = 1;
-                sh.pub_image[issued % kPubRing] = it.image;
-                sh.pub_pass[issued % kPubRing] = it.pass;
-                float2 *stage = stages + (size_t)s * kStageElems;
-                if (ps.along_rows) {
-                    const int n = im.cols, lines = tile_px / n;
-                    const int row0 = it.tile * lines;
-                    const int nrows = min(lines, im.rows - row0);
-                    const unsigned bytes = (unsigned)(nrows * n * sizeof(float2));
-                    const float2 *src = (it.pass == 0 ? im.src : im.dst) + (size_t)row0 * n;
-                    mbar_arrive_tx(&sh.full[s], bytes);
-                    bulk_g2s(stage, src, bytes, &sh.full[s]);
-                } else {
-                    const int n = im.rows, w = tile_px / n;
-                    const int br = n < 256 ? n : 256;
-                    const void *tmap =
-                        static_cast<const unsigned char *>(a.tmaps) + (size_t)it.image * 128;
-                    mbar_arrive_tx(&sh.full[s], (unsigned)(n * w * sizeof(float2)));
-                    for (int b = 0; b < n / br; b++)
-                        tensor2d_g2s(stage + (size_t)b * br * w, tmap, it.tile * w, b * br,
-                                     &sh.full[s]);
-                }
-                issued++;
-                store_ready();
             }
-            if (failed || done) break;
-            if (!a.claim_ahead) claim = atomicAdd(a.head, (unsigned)chunk);
+            // the stage's previous item must be computed and its store
+            // must have read the stage before the stage is refilled
+            const unsigned long long tr0 = a.stats ? gtimer() : 0;
+            if (issued >= ST) {
+                const int j = issued - ST;
+                while (stored <= j) {
+                    if (!mbar_wait(&sh.computed[stored % ST], (stored / ST) & 1, a.wait_limit_ns))
+                        return false;
+                    store_ready();
+                }
+                const int newer = stored - j - 1;
+                if (newer >= 2) bulk_wait_read<2>();
+                else if (newer == 1) bulk_wait_read<1>();
+                else bulk_wait_read<0>();
+            }
+            if (a.stats) sh.st[BS_REFILL_WAIT] += gtimer() - tr0;
+            // publish what has surely landed; never let the ring overflow
+            if (issued - published >= kPubRing) complete_upto(issued - kPubRing + 1);
+            if (stored - 2 > published) complete_upto(stored - 2);
+            StageInfo &inf = sh.info[s];
+            if (!itp) {  // queue exhausted: tell the compute warps to stop
+                inf.valid = 0;
+                mbar_arrive(&sh.full[s]);
+                return true;
+            }
+            const BatchItem &it = *itp;
+            inf.dst = im.dst;
+            inf.rows = im.rows;
+            inf.cols = im.cols;
+            inf.tile = it.tile;
+            inf.image = it.image;
+            inf.pass = it.pass;
+            inf.along_rows = ps.along_rows;
+            inf.flags = ps.flags;
+            inf.scale = ps.scale;
+            inf.valid = 1;
+            sh.pub_image[issued % kPubRing] = it.image;
+            sh.pub_pass[issued % kPubRing] = it.pass;
+            float2 *stage = stages + (size_t)s * kStageElems;
+            if (ps.along_rows) {
+                const int n = im.cols, lines = tile_px / n;
+                const int row0 = it.tile * lines;
+                const int nrows = min(lines, im.rows - row0);
+                const unsigned bytes = (unsigned)(nrows * n * sizeof(float2));
+                const float2 *src = (it.pass == 0 ? im.src : im.dst) + (size_t)row0 * n;
+                mbar_arrive_tx(&sh.full[s], bytes);
+                bulk_g2s(stage, src, bytes, &sh.full[s]);
+            } else {
+                const int n = im.rows, w = tile_px / n;
+                const int br = n < 256 ? n : 256;
+                const void *tmap = static_cast<const unsigned char *>(a.tmaps) + (size_t)it.image * 128;
+                mbar_arrive_tx(&sh.full[s], (unsigned)(n * w * sizeof(float2)));
+                for (int b = 0; b < n / br; b++)
+                    tensor2d_g2s(stage + (size_t)b * br * w, tmap, it.tile * w, b * br, &sh.full[s]);
+            }
+            issued++;
+            store_ready();
+            return true;
+        };
+
+        if (a.claim_ahead >= 2) {
+            // Deep prefetch, one item per claim: item k+3 is claimed, item
+            // k+2's record fetched, and item k+1's image record and
+            // dependency counter read, while item k is issued -- each load
+            // has a whole item's time to arrive.
+            const unsigned n = (unsigned)a.n_items;
+            const unsigned none = 0xffffffffu;
+            unsigned c0 = atomicAdd(a.head, 1u), c1 = atomicAdd(a.head, 1u);
+            unsigned c2 = atomicAdd(a.head, 1u);
+            BatchItem r0{}, r1{};
+            if (c0 < n) r0 = a.items[c0];
+            if (c1 < n) r1 = a.items[c1];
+            BatchImage i0{};
+            unsigned s0 = none;
+            if (c0 < n) {
+                i0 = a.images[r0.image];
+                if (r0.pass > 0) s0 = ld_relaxed_u32(a.done + r0.image * kBatchMaxPasses + r0.pass - 1);
+            }
+            int err = 0;
+            for (;;) {
+                if (c0 >= n || err) {
+                    if (!issue_item(nullptr, nullptr, none)) failed = true;
+                    break;
+                }
+                // advance the pipeline: claim k+3, fetch k+2's record, look
+                // at k+1's image record and dependency, read the error flag
+                const unsigned c3 = c2 < n ? atomicAdd(a.head, 1u) : n;
+                BatchItem r2{};
+                if (c2 < n) r2 = a.items[c2];
+                BatchImage i1{};
+                unsigned s1 = none;
+                if (c1 < n) {
+                    i1 = a.images[r1.image];
+                    if (r1.pass > 0)
+                        s1 = ld_relaxed_u32(a.done + r1.image * kBatchMaxPasses + r1.pass - 1);
+                }
+                const int err1 = ld_relaxed_s32(a.error);
+                if (!issue_item(&r0, &i0, s0)) {
+                    failed = true;
+                    break;
+                }
+                c0 = c1;
+                c1 = c2;
+                c2 = c3;
+                r0 = r1;
+                r1 = r2;
+                i0 = i1;
+                s0 = s1;
+                err = err1;
+            }
+        } else {
+            const int chunk =
+                a.claim_chunk < 1 ? 1 : (a.claim_chunk > kChunk ? kChunk : a.claim_chunk);
+            unsigned claim = atomicAdd(a.head, (unsigned)chunk);
+            for (;;) {
+                const int base = (int)claim;
+                const bool done = base >= a.n_items || *(volatile int *)a.error;
+                if (!done && a.claim_ahead) claim = atomicAdd(a.head, (unsigned)chunk);  // in flight
+                const int cnt = done ? 0 : min(chunk, a.n_items - base);
+                BatchItem its[kChunk];
+#pragma unroll
+                for (int q = 0; q < kChunk; q++)
+                    if (q < cnt) its[q] = a.items[base + q];
+                for (int q = 0; q < cnt && !failed; q++)
+                    if (!issue_item(&its[q], nullptr, 0xffffffffu)) failed = true;
+                if (!failed && done && !issue_item(nullptr, nullptr, 0xffffffffu)) failed = true;
+                if (failed || done) break;
+                if (!a.claim_ahead) claim = atomicAdd(a.head, (unsigned)chunk);
+            }
         }
         if (failed) {
             atomicExch(a.error, GLSFFT_ERROR_TIMEOUT);
@@ -496,18 +583,29 @@ __global__ void __launch_bounds__(kBlock, MINB) fft_batch_ws(BatchArgs a) {
         bulk_wait<0>();
         asm volatile("fence.proxy.async.global;" ::: "memory");
         if (drain_ok) publish_upto(stored);
+        if (a.stats) {
+            atomicAdd(a.stats + BS_DEP_WAIT, sh.st[BS_DEP_WAIT]);
+            atomicAdd(a.stats + BS_REFILL_WAIT, sh.st[BS_REFILL_WAIT]);
+            atomicAdd(a.stats + BS_PUBLISH_WAIT, sh.st[BS_PUBLISH_WAIT]);
+            atomicAdd(a.stats + BS_PRODUCER_TOTAL, gtimer() - sh.st[BS_PRODUCER_TOTAL]);
+            atomicAdd(a.stats + BS_ITEMS, (unsigned long long)issued);
+            atomicAdd(a.stats + BS_BLOCKS, 1ull);
+        }
         return;
     }
 
     // ------------------------------------------------------------ compute
     const int tid = threadIdx.x;
     int cached_n = -1;
+    if (a.stats && tid == 0) sh.st[BS_COMPUTE_TOTAL] = gtimer();
     for (int k = 0;; k++) {
         const int s = k % ST;
+        const unsigned long long tf0 = (a.stats && tid == 0) ? gtimer() : 0;
         if (!mbar_wait(&sh.full[s], (k / ST) & 1, a.wait_limit_ns)) {
             if (tid == 0) atomicExch(a.error, GLSFFT_ERROR_TIMEOUT);
             break;
         }
+        if (a.stats && tid == 0) sh.st[BS_FULL_WAIT] += gtimer() - tf0;
         const StageInfo in = sh.info[s];
         if (!in.valid) break;
         ws_compute(stages + (size_t)s * kStageElems, in, a.tw, twc, tid, cached_n);
@@ -515,6 +613,10 @@ __global__ void __launch_bounds__(kBlock, MINB) fft_batch_ws(BatchArgs a) {
         // producer's TMA store (and the next TMA write into the stage)
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         mbar_arrive(&sh.computed[s]);
+    }
+    if (a.stats && tid == 0) {
+        atomicAdd(a.stats + BS_FULL_WAIT, sh.st[BS_FULL_WAIT]);
+        atomicAdd(a.stats + BS_COMPUTE_TOTAL, gtimer() - sh.st[BS_COMPUTE_TOTAL]);
     }
 }
 

@@ -198,8 +198,8 @@ GLSFFT_API int glsfft_batch_execute(glsfft_batch plan, void *stream);
  * 1 = warp-specialised: a producer warp stages tiles with TMA into a 3-stage
  *     shared-memory ring for 8 compute warps and writes the results back
  *     with TMA stores (1 block/SM);
- * 2 = the same at 2 blocks/SM (the default);
- * 3 = the same at 3 blocks/SM with a 2-stage ring.
+ * 2 = the same at 2 blocks/SM;
+ * 3 = the same at 3 blocks/SM with a 2-stage ring (the default).
  */
 #define GLSFFT_BATCH_PLAIN 0
 #define GLSFFT_BATCH_TMA_WS1 1
@@ -209,10 +209,13 @@ GLSFFT_API int glsfft_batch_set_variant(glsfft_batch plan, int variant);
 
 /*
  * Work-queue schedule of a plan (re-captures its graph): items claimed per
- * queue atomic by a warp-specialised block (1..4), whether it claims the next
- * batch of items before starting the current one, and the item-list lag
- * (items listed between an image's pass and its next pass; 0 keeps the
- * current order).  Defaults: 2, 0, four resident grids.
+ * queue atomic by a warp-specialised block (1..4); claim_ahead 0 = claim the
+ * next batch of items after finishing the current one, 1 = before starting
+ * it, 2 = deep prefetch (one item per claim; the item three ahead is
+ * claimed, two ahead fetched, the next one's image record and dependency
+ * counter read while an item is issued); and the item-list lag (items
+ * listed between an image's pass and its next pass; 0 keeps the current
+ * order).  Defaults: 2, 0, eight resident grids.
  */
 GLSFFT_API int glsfft_batch_set_schedule(glsfft_batch plan, int claim_chunk, int claim_ahead,
                                          int lag_items);
@@ -243,7 +246,7 @@ GLSFFT_API int glsfft_batch_get_schedule(glsfft_batch plan, int *schedule4);
  * that get their own pass launches have their per-size pass schedules tuned
  * (glsfft_autotune_fft2d).  Then every persistent-kernel schedule -- variant
  * (GLSFFT_BATCH_*) x item-order lag (1, 2, 4, 8 resident grids) x claim
- * chunk (1, 2, 4) x claim-ahead (0, 1), 76 in all -- is timed, `reps` graph launches
+ * chunk and claim-ahead ((1, 2, 4) x (0, 1), and 1 x 2), 88 in all -- is timed, `reps` graph launches
  * each (median, CUDA events on `stream`), on a shadow plan of the same
  * shapes, flags, alignments and aliasing over scratch buffers, so the
  * plan's own images are never read or written.  The fastest is applied to
@@ -257,6 +260,28 @@ GLSFFT_API int glsfft_batch_get_schedule(glsfft_batch plan, int *schedule4);
  */
 GLSFFT_API int glsfft_batch_autotune(glsfft_batch plan, const char *cache_path, int reps,
                                      void *stream, int *result, double *ms);
+
+/*
+ * The last glsfft_batch_autotune search of this plan (timed there, not from
+ * the cache): *count candidates; the first `max` are written as
+ * sched4[4i..4i+3] = {variant, claim_chunk, claim_ahead, lag in resident
+ * grids} and ms[i] = median time per execution.
+ */
+GLSFFT_API int glsfft_batch_tuning(glsfft_batch plan, int max, int *sched4, double *ms,
+                                   int *count);
+
+/*
+ * Timing counters of the warp-specialised kernels (no reference
+ * counterpart; off by default, re-captures the graph).  While on, every
+ * execution adds, summed over blocks, in nanoseconds: [0] producer time in
+ * dependency waits, [1] in waits for a stage to be free, [2] in store
+ * completion waits before publishing, [3] producer run time, [4] compute
+ * warp 0's waits for staged tiles, [5] its run time; [6] items, [7] blocks.
+ * glsfft_batch_get_stats synchronises `stream`, returns the sums (8
+ * doubles) and resets them.
+ */
+GLSFFT_API int glsfft_batch_set_stats(glsfft_batch plan, int on);
+GLSFFT_API int glsfft_batch_get_stats(glsfft_batch plan, void *stream, double *out8);
 
 GLSFFT_API int glsfft_batch_destroy(glsfft_batch plan);
 
