@@ -1,9 +1,10 @@
 // batch_ws.cu -- warp-specialised persistent batched FFT with TMA staging.
 //
-// Block = 8 compute warps + 1 producer warp.  The producer (one lane) pulls
-// (image, pass, tile) items from the plan's work list, waits (bounded) until
-// the image's previous pass is complete, and stages the tile into one of
-// three shared-memory buffers with the Tensor Memory Accelerator:
+// Block = 8 compute warps + a loader warp + a storer warp (one active lane
+// each).  The loader pulls (image, pass, tile) items from the plan's work
+// list, waits (bounded) until the image's previous pass is complete, and
+// stages the tile into a shared-memory ring with the Tensor Memory
+// Accelerator:
 //   * a rows tile (LINES contiguous rows) is one cp.async.bulk copy;
 //   * a columns tile (W adjacent columns x N rows, W*8 = 32..512 bytes per
 //     row) is read as 2-D boxes through a per-image tensor map
@@ -13,15 +14,14 @@
 // warps read their 16 values per thread from the stage, run the Stockham
 // passes (exchanging through the same buffer), write the results back into
 // the stage in the image's layout and arrive on the stage's "computed"
-// mbarrier.  The producer then writes the tile out with the TMA as well (one
-// cp.async.bulk for a rows tile, 2-D tensor boxes for a columns tile), so the
-// compute warps issue no global stores.  Before the stage is refilled the
-// store's bulk group must be complete; the producer then publishes the tile
-// (release fence + counter).  Items are stored and published in order, and
-// the producer completes and publishes every stored tile while it waits on a
-// dependency, so no block ever holds back the work another waits for.  Every
-// wait is bounded: on expiry the block records GLSFFT_ERROR_TIMEOUT, lets
-// the compute warps drain, waits for its own copies and exits.
+// mbarrier.  The storer writes the tile out with the TMA (one cp.async.bulk
+// for a rows tile, 2-D tensor boxes for a columns tile), arrives on the
+// stage's "empty" mbarrier as soon as the store has read the stage (the
+// loader then refills it), waits for the store's writes and publishes the
+// tile at once (release fence + counter), so dependent passes never wait on
+// a block's later work.  Every wait is bounded: on expiry the block records
+// GLSFFT_ERROR_TIMEOUT, lets the compute warps drain, waits for its own
+// copies and exits.
 #include <cuda.h>
 
 #include "batch_internal.h"
@@ -34,7 +34,9 @@ namespace glsfft {
 namespace {
 
 constexpr int kCompute = 256;                      // compute threads
-constexpr int kBlock = kCompute + 32;              // + producer warp
+constexpr int kLoaderWarp = kCompute / 32;         // warp 8
+constexpr int kStorerWarp = kCompute / 32 + 1;     // warp 9
+constexpr int kBlock = kCompute + 64;              // + loader and storer warps
 constexpr int kStageElems = 4352;                  // padded_count(4096)
 constexpr size_t kStageBytes = kStageElems * sizeof(float2);
 
@@ -46,17 +48,12 @@ struct StageInfo {
     int pad[5];
 };
 
-// Items stored but not yet published keep their (image, pass) here, since
-// their stage may already hold a later item.
-constexpr int kPubRing = 8;
-
 template <int ST>
 struct WsShared {
-    unsigned long long full[ST];
-    unsigned long long computed[ST];
+    unsigned long long full[ST];      // tile staged (TMA transaction bytes)
+    unsigned long long computed[ST];  // results in the stage (256 compute arrivals)
+    unsigned long long empty[ST];     // the store has read the stage (storer)
     StageInfo info[ST];
-    int pub_image[kPubRing];
-    int pub_pass[kPubRing];
     unsigned long long st[6];  // timing sums when BatchArgs::stats is set (BS_* order)
 };
 
@@ -92,15 +89,6 @@ __device__ __forceinline__ void mbar_arrive_tx(unsigned long long *b, unsigned b
                      smem_u32(b)),
                  "r"(bytes)
                  : "memory");
-}
-__device__ __forceinline__ bool mbar_test(unsigned long long *b, unsigned parity) {
-    unsigned ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\tmbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(ok)
-        : "r"(smem_u32(b)), "r"(parity)
-        : "memory");
-    return ok != 0;
 }
 // One try_wait: the thread may be suspended (not spinning on issue slots)
 // until the phase completes or a hardware time limit passes.
@@ -293,87 +281,35 @@ __device__ __forceinline__ void ws_compute(float2 *stage, const StageInfo &in, c
 template <int MINB, int ST>
 __global__ void __launch_bounds__(kBlock, MINB) fft_batch_ws(BatchArgs a) {
     extern __shared__ __align__(128) unsigned char ws_raw[];
-    // 128-byte aligned stage buffers, then the barriers and stage records
+    // 128-byte aligned stage buffers, the twiddle cache, then the barriers
+    // and stage records
     unsigned char *base = reinterpret_cast<unsigned char *>(
         (reinterpret_cast<uintptr_t>(ws_raw) + 127) & ~uintptr_t(127));
     float2 *stages = reinterpret_cast<float2 *>(base);
     float4 *twc = reinterpret_cast<float4 *>(base + ST * kStageBytes);
     WsShared<ST> &sh = *reinterpret_cast<WsShared<ST> *>(base + ST * kStageBytes +
-                                                 kTwCacheF4 * sizeof(float4));
+                                                         kTwCacheF4 * sizeof(float4));
 
     if (threadIdx.x == 0) {
         for (int i = 0; i < 6; i++) sh.st[i] = 0;
         for (int s = 0; s < ST; s++) {
             mbar_init(&sh.full[s], 1);
             mbar_init(&sh.computed[s], kCompute);
+            mbar_init(&sh.empty[s], 1);
         }
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
+    const int warp = threadIdx.x / 32;
 
-    if (threadIdx.x >= kCompute) {
-        // ------------------------------------------------------ producer
-        if (threadIdx.x != kCompute) return;
+    if (warp == kLoaderWarp) {
+        // -------------------------------------------------------- loader
+        if (threadIdx.x % 32 != 0) return;
         const int tile_px = kBatchTileElems;
-        // optional timing sums (BatchArgs::stats), kept in shared memory
-        if (a.stats) sh.st[BS_PRODUCER_TOTAL] = gtimer();
         constexpr int kChunk = 4;  // items claimed per queue atomic
-        int issued = 0, stored = 0, published = 0;
+        if (a.stats) sh.st[BS_PRODUCER_TOTAL] = gtimer();
+        int issued = 0;
         bool failed = false;
-        // Publish the items [published, end) in order: one release fence,
-        // then one counter add per run of the same (image, pass), from the
-        // publication ring (at most kPubRing items are ever unpublished).
-        auto publish_upto = [&](int end) {
-            if (end <= published) return;
-            asm volatile("fence.acq_rel.gpu;" ::: "memory");
-            while (published < end) {
-                const int img = sh.pub_image[published % kPubRing];
-                const int pas = sh.pub_pass[published % kPubRing];
-                unsigned n = 0;
-                while (published < end && sh.pub_image[published % kPubRing] == img &&
-                       sh.pub_pass[published % kPubRing] == pas) {
-                    published++;
-                    n++;
-                }
-                atomicAdd(a.done + img * kBatchMaxPasses + pas, n);
-            }
-        };
-        // the TMA store of item j, whose results are in stage j % ST
-        auto store_item = [&](int j) {
-            const StageInfo &inf = sh.info[j % ST];
-            const float2 *stage = stages + (size_t)(j % ST) * kStageElems;
-            if (inf.along_rows) {
-                const int n = inf.cols, lines = tile_px / n, row0 = inf.tile * lines;
-                const int nrows = min(lines, inf.rows - row0);
-                bulk_s2g(inf.dst + (size_t)row0 * n, stage, (unsigned)(nrows * n * sizeof(float2)));
-            } else {
-                const int n = inf.rows, w = tile_px / n, br = n < 256 ? n : 256;
-                const void *tmap = static_cast<const unsigned char *>(a.tmaps) + (size_t)inf.image * 128;
-                for (int b = 0; b < n / br; b++)
-                    tensor2d_s2g(tmap, inf.tile * w, b * br, stage + (size_t)b * br * w);
-            }
-            bulk_commit();
-        };
-        // store every item the compute warps have finished, in order (no wait)
-        auto store_ready = [&]() {
-            while (stored < issued &&
-                   mbar_test(&sh.computed[stored % ST], (stored / ST) & 1))
-                store_item(stored++);
-        };
-        // complete the stores of items [published, end) (end <= stored) and
-        // publish them; stores issued after item end-1 may stay in flight
-        auto complete_upto = [&](int end) {
-            if (end <= published) return;
-            const unsigned long long tw0 = a.stats ? gtimer() : 0;
-            const int newer = stored - end;
-            if (newer >= 2) bulk_wait<2>();
-            else if (newer == 1) bulk_wait<1>();
-            else bulk_wait<0>();
-            // the async-proxy writes are complete: order them before the release
-            asm volatile("fence.proxy.async.global;" ::: "memory");
-            if (a.stats) sh.st[BS_PUBLISH_WAIT] += gtimer() - tw0;
-            publish_upto(end);
-        };
         int cur_img = -1, cur_pass = -1, cur_need = -1;
         bool dep_ok = false;
         BatchImage im{};
@@ -406,48 +342,33 @@ __global__ void __launch_bounds__(kBlock, MINB) fft_batch_ws(BatchArgs a) {
                     // every tile of this image's previous pass must be published
                     const unsigned *cnt_p = a.done + it.image * kBatchMaxPasses + it.pass - 1;
                     const unsigned long long t0 = gtimer();
-                    const unsigned long long pub0 = a.stats ? sh.st[BS_PUBLISH_WAIT] : 0;
                     bool ok = true;
                     while (ld_acquire_u32(cnt_p) < (unsigned)it.need) {
-                        store_ready();
-                        complete_upto(stored);
                         if ((long long)(gtimer() - t0) > a.wait_limit_ns) {
                             ok = false;
                             break;
                         }
-                        __nanosleep(128);
+                        __nanosleep(64);
                     }
-                    if (a.stats)
-                        sh.st[BS_DEP_WAIT] += gtimer() - t0 - (sh.st[BS_PUBLISH_WAIT] - pub0);
+                    if (a.stats) sh.st[BS_DEP_WAIT] += gtimer() - t0;
                     if (!ok) return false;
                     // order the acquire before the async-proxy (TMA) reads
                     asm volatile("fence.proxy.async.global;" ::: "memory");
                     dep_ok = true;
                 }
             }
-            // the stage's previous item must be computed and its store
-            // must have read the stage before the stage is refilled
-            const unsigned long long tr0 = a.stats ? gtimer() : 0;
+            // the store of the stage's previous item must have read it
             if (issued >= ST) {
+                const unsigned long long tr0 = a.stats ? gtimer() : 0;
                 const int j = issued - ST;
-                while (stored <= j) {
-                    if (!mbar_wait(&sh.computed[stored % ST], (stored / ST) & 1, a.wait_limit_ns))
-                        return false;
-                    store_ready();
-                }
-                const int newer = stored - j - 1;
-                if (newer >= 2) bulk_wait_read<2>();
-                else if (newer == 1) bulk_wait_read<1>();
-                else bulk_wait_read<0>();
+                if (!mbar_wait(&sh.empty[s], (j / ST) & 1, a.wait_limit_ns)) return false;
+                if (a.stats) sh.st[BS_REFILL_WAIT] += gtimer() - tr0;
             }
-            if (a.stats) sh.st[BS_REFILL_WAIT] += gtimer() - tr0;
-            // publish what has surely landed; never let the ring overflow
-            if (issued - published >= kPubRing) complete_upto(issued - kPubRing + 1);
-            if (stored - 2 > published) complete_upto(stored - 2);
             StageInfo &inf = sh.info[s];
-            if (!itp) {  // queue exhausted: tell the compute warps to stop
+            if (!itp) {  // queue exhausted: tell the compute warps and the storer to stop
                 inf.valid = 0;
                 mbar_arrive(&sh.full[s]);
+                issued++;
                 return true;
             }
             const BatchItem &it = *itp;
@@ -461,8 +382,6 @@ __global__ void __launch_bounds__(kBlock, MINB) fft_batch_ws(BatchArgs a) {
             inf.flags = ps.flags;
             inf.scale = ps.scale;
             inf.valid = 1;
-            sh.pub_image[issued % kPubRing] = it.image;
-            sh.pub_pass[issued % kPubRing] = it.pass;
             float2 *stage = stages + (size_t)s * kStageElems;
             if (ps.along_rows) {
                 const int n = im.cols, lines = tile_px / n;
@@ -481,7 +400,6 @@ __global__ void __launch_bounds__(kBlock, MINB) fft_batch_ws(BatchArgs a) {
                     tensor2d_g2s(stage + (size_t)b * br * w, tmap, it.tile * w, b * br, &sh.full[s]);
             }
             issued++;
-            store_ready();
             return true;
         };
 
@@ -509,8 +427,6 @@ __global__ void __launch_bounds__(kBlock, MINB) fft_batch_ws(BatchArgs a) {
                     if (!issue_item(nullptr, nullptr, none)) failed = true;
                     break;
                 }
-                // advance the pipeline: claim k+3, fetch k+2's record, look
-                // at k+1's image record and dependency, read the error flag
                 const unsigned c3 = c2 < n ? atomicAdd(a.head, 1u) : n;
                 BatchItem r2{};
                 if (c2 < n) r2 = a.items[c2];
@@ -540,14 +456,14 @@ __global__ void __launch_bounds__(kBlock, MINB) fft_batch_ws(BatchArgs a) {
                 a.claim_chunk < 1 ? 1 : (a.claim_chunk > kChunk ? kChunk : a.claim_chunk);
             unsigned claim = atomicAdd(a.head, (unsigned)chunk);
             for (;;) {
-                const int base = (int)claim;
-                const bool done = base >= a.n_items || *(volatile int *)a.error;
+                const int base_i = (int)claim;
+                const bool done = base_i >= a.n_items || *(volatile int *)a.error;
                 if (!done && a.claim_ahead) claim = atomicAdd(a.head, (unsigned)chunk);  // in flight
-                const int cnt = done ? 0 : min(chunk, a.n_items - base);
+                const int cnt = done ? 0 : min(chunk, a.n_items - base_i);
                 BatchItem its[kChunk];
 #pragma unroll
                 for (int q = 0; q < kChunk; q++)
-                    if (q < cnt) its[q] = a.items[base + q];
+                    if (q < cnt) its[q] = a.items[base_i + q];
                 for (int q = 0; q < cnt && !failed; q++)
                     if (!issue_item(&its[q], nullptr, 0xffffffffu)) failed = true;
                 if (!failed && done && !issue_item(nullptr, nullptr, 0xffffffffu)) failed = true;
@@ -557,40 +473,65 @@ __global__ void __launch_bounds__(kBlock, MINB) fft_batch_ws(BatchArgs a) {
         }
         if (failed) {
             atomicExch(a.error, GLSFFT_ERROR_TIMEOUT);
-            // the compute warps finish what was issued, then stop here (the
-            // stage's previous item is let finish first, bounded)
-            if (issued >= ST && stored <= issued - ST)
-                mbar_wait(&sh.computed[(issued - ST) % ST],
-                          ((issued - ST) / ST) & 1, a.wait_limit_ns);
+            // no copy into this block's shared memory may still be in flight
+            // when the block exits: wait (bounded) for the last loads issued
+            for (int k = issued > ST ? issued - ST : 0; k < issued; k++)
+                mbar_wait(&sh.full[k % ST], (k / ST) & 1, a.wait_limit_ns);
+            // stop the compute warps and the storer after what was issued
+            // (the stage is let drain first, bounded)
             const int s = issued % ST;
+            if (issued >= ST) mbar_wait(&sh.empty[s], ((issued - ST) / ST) & 1, a.wait_limit_ns);
             sh.info[s].valid = 0;
             mbar_arrive(&sh.full[s]);
         }
-        // store and publish what is left; make sure no copy into or out of
-        // this block's shared memory is in flight when the block exits
-        bool drain_ok = !failed;
-        while (stored < issued) {
-            const int j = stored;
-            if (drain_ok && mbar_wait(&sh.computed[j % ST], (j / ST) & 1, a.wait_limit_ns)) {
-                store_item(j);
-            } else {
-                drain_ok = false;
-                atomicExch(a.error, GLSFFT_ERROR_TIMEOUT);
-                mbar_wait(&sh.full[j % ST], (j / ST) & 1, a.wait_limit_ns);
-            }
-            stored++;
-        }
-        bulk_wait<0>();
-        asm volatile("fence.proxy.async.global;" ::: "memory");
-        if (drain_ok) publish_upto(stored);
         if (a.stats) {
             atomicAdd(a.stats + BS_DEP_WAIT, sh.st[BS_DEP_WAIT]);
             atomicAdd(a.stats + BS_REFILL_WAIT, sh.st[BS_REFILL_WAIT]);
-            atomicAdd(a.stats + BS_PUBLISH_WAIT, sh.st[BS_PUBLISH_WAIT]);
             atomicAdd(a.stats + BS_PRODUCER_TOTAL, gtimer() - sh.st[BS_PRODUCER_TOTAL]);
             atomicAdd(a.stats + BS_ITEMS, (unsigned long long)issued);
             atomicAdd(a.stats + BS_BLOCKS, 1ull);
         }
+        return;
+    }
+
+    if (warp == kStorerWarp) {
+        // -------------------------------------------------------- storer
+        if (threadIdx.x % 32 != 0) return;
+        const int tile_px = kBatchTileElems;
+        unsigned long long st_pub = 0;
+        for (int j = 0;; j++) {
+            const int s = j % ST;
+            if (!mbar_wait(&sh.computed[s], (j / ST) & 1, a.wait_limit_ns)) {
+                atomicExch(a.error, GLSFFT_ERROR_TIMEOUT);
+                break;
+            }
+            const StageInfo inf = sh.info[s];
+            if (!inf.valid) break;
+            const float2 *stage = stages + (size_t)s * kStageElems;
+            if (inf.along_rows) {
+                const int n = inf.cols, lines = tile_px / n, row0 = inf.tile * lines;
+                const int nrows = min(lines, inf.rows - row0);
+                bulk_s2g(inf.dst + (size_t)row0 * n, stage, (unsigned)(nrows * n * sizeof(float2)));
+            } else {
+                const int n = inf.rows, w = tile_px / n, br = n < 256 ? n : 256;
+                const void *tmap =
+                    static_cast<const unsigned char *>(a.tmaps) + (size_t)inf.image * 128;
+                for (int b = 0; b < n / br; b++)
+                    tensor2d_s2g(tmap, inf.tile * w, b * br, stage + (size_t)b * br * w);
+            }
+            bulk_commit();
+            const unsigned long long tw0 = a.stats ? gtimer() : 0;
+            bulk_wait_read<0>();        // the stage may be refilled
+            mbar_arrive(&sh.empty[s]);
+            bulk_wait<0>();             // the tile is in global memory
+            // the async-proxy writes are complete: order them before the release
+            asm volatile("fence.proxy.async.global;" ::: "memory");
+            asm volatile("fence.acq_rel.gpu;" ::: "memory");
+            atomicAdd(a.done + inf.image * kBatchMaxPasses + inf.pass, 1u);
+            if (a.stats) st_pub += gtimer() - tw0;
+        }
+        bulk_wait<0>();
+        if (a.stats) atomicAdd(a.stats + BS_PUBLISH_WAIT, st_pub);
         return;
     }
 
@@ -607,12 +548,13 @@ __global__ void __launch_bounds__(kBlock, MINB) fft_batch_ws(BatchArgs a) {
         }
         if (a.stats && tid == 0) sh.st[BS_FULL_WAIT] += gtimer() - tf0;
         const StageInfo in = sh.info[s];
-        if (!in.valid) break;
-        ws_compute(stages + (size_t)s * kStageElems, in, a.tw, twc, tid, cached_n);
+        if (in.valid) ws_compute(stages + (size_t)s * kStageElems, in, a.tw, twc, tid, cached_n);
         // the generic-proxy writes of the results are ordered before the
-        // producer's TMA store (and the next TMA write into the stage)
+        // storer's TMA store (and the next TMA write into the stage); the
+        // stop record is passed on to the storer the same way
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         mbar_arrive(&sh.computed[s]);
+        if (!in.valid) break;
     }
     if (a.stats && tid == 0) {
         atomicAdd(a.stats + BS_FULL_WAIT, sh.st[BS_FULL_WAIT]);
