@@ -25,8 +25,32 @@
 namespace glsfft {
 
 // ------------------------------------------------------------ complex helpers
-__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
-__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+// Complex add / subtract as one packed FP32x2 instruction (sm_100 family);
+// each lane rounds exactly like the scalar operation.
+__device__ __forceinline__ unsigned long long f2_bits(float2 a) {
+    return *reinterpret_cast<unsigned long long *>(&a);
+}
+__device__ __forceinline__ float2 bits_f2(unsigned long long u) {
+    return *reinterpret_cast<float2 *>(&u);
+}
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) {
+    unsigned long long d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(f2_bits(a)), "l"(f2_bits(b)));
+    return bits_f2(d);
+}
+__device__ __forceinline__ float2 csub(float2 a, float2 b) {
+    unsigned long long d;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(f2_bits(a)), "l"(f2_bits(b)));
+    return bits_f2(d);
+}
+// a + (s.x * b.y, s.y * b.x) for s = (+-1, +-1): a +- i*b in one packed FMA
+// (the products by +-1 are exact, so each lane equals the scalar add/sub)
+__device__ __forceinline__ float2 cadd_swapped(float2 a, float2 b, float2 s) {
+    unsigned long long d;
+    const float2 bs = make_float2(b.y, b.x);
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(f2_bits(bs)), "l"(f2_bits(s)), "l"(f2_bits(a)));
+    return bits_f2(d);
+}
 // Complex product with explicit fused multiply-adds: every kernel that
 // inlines it rounds the same way, whatever contraction the compiler would
 // choose, so the batch, pass and plain kernels give bit-identical lines.
@@ -100,8 +124,8 @@ template <> struct Dft<4> {
         float2 bpd = cadd(v[1], v[3]), bmd = csub(v[1], v[3]);
         v[0] = cadd(apc, bpd);
         v[2] = csub(apc, bpd);
-        v[1] = make_float2(amc.x + bmd.y, amc.y - bmd.x);  // amc - i*bmd
-        v[3] = make_float2(amc.x - bmd.y, amc.y + bmd.x);  // amc + i*bmd
+        v[1] = cadd_swapped(amc, bmd, make_float2(1.f, -1.f));  // amc - i*bmd
+        v[3] = cadd_swapped(amc, bmd, make_float2(-1.f, 1.f));  // amc + i*bmd
     }
 };
 template <> struct Dft<8> {
