@@ -545,7 +545,7 @@ int glsfft_batch_autotune(glsfft_batch plan, const char *cache_path, int reps, v
     using Cand = glsfft_batch_s::Cand;
     std::vector<Cand> cands;
     const int variants[4] = {BATCH_TMA_WS2, BATCH_TMA_WS3, BATCH_TMA_WS1, BATCH_PLAIN};
-    const int lags[4] = {1, 2, 4, 8};
+    const int lags[6] = {2, 3, 4, 5, 6, 8};
     for (int v : variants) {
         for (int lg : lags) {
             for (int c = 1; c <= 4 && !st; c *= 2) {

@@ -51,6 +51,12 @@ __device__ __forceinline__ float2 cadd_swapped(float2 a, float2 b, float2 s) {
     asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(f2_bits(bs)), "l"(f2_bits(s)), "l"(f2_bits(a)));
     return bits_f2(d);
 }
+// (a.x * sx, a.y * sy) as one packed multiply
+__device__ __forceinline__ float2 cmul_re(float2 a, float sx, float sy) {
+    unsigned long long d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(f2_bits(a)), "l"(f2_bits(make_float2(sx, sy))));
+    return bits_f2(d);
+}
 // Complex product with explicit fused multiply-adds: every kernel that
 // inlines it rounds the same way, whatever contraction the compiler would
 // choose, so the batch, pass and plain kernels give bit-identical lines.
@@ -93,10 +99,16 @@ __device__ __forceinline__ float2 wmul(float2 v) {
     else if constexpr (k16 == 4) return make_float2(v.y, -v.x);
     else if constexpr (k16 == 8) return make_float2(-v.x, -v.y);
     else if constexpr (k16 == 12) return make_float2(-v.y, v.x);
-    else if constexpr (k16 == 2) return make_float2((v.x + v.y) * S, (v.y - v.x) * S);
-    else if constexpr (k16 == 6) return make_float2((v.y - v.x) * S, -(v.x + v.y) * S);
-    else if constexpr (k16 == 10) return make_float2(-(v.x + v.y) * S, (v.x - v.y) * S);
-    else if constexpr (k16 == 14) return make_float2((v.x - v.y) * S, (v.x + v.y) * S);
+    // odd multiples of pi/4: the sum and difference of the components, then
+    // one packed multiply (each lane rounds like the scalar expression)
+    else if constexpr (k16 == 2) return cmul_re(cadd_swapped(v, v, make_float2(1.f, -1.f)), S, S);
+    else if constexpr (k16 == 6) {
+        const float2 t = cadd_swapped(v, v, make_float2(1.f, -1.f));  // (x+y, y-x)
+        return cmul_re(make_float2(t.y, t.x), S, -S);
+    } else if constexpr (k16 == 10) {
+        const float2 t = cadd_swapped(v, v, make_float2(-1.f, 1.f));  // (x-y, y+x)
+        return cmul_re(make_float2(t.y, t.x), -S, S);
+    } else if constexpr (k16 == 14) return cmul_re(cadd_swapped(v, v, make_float2(-1.f, 1.f)), S, S);
     else {
         // odd multiples of pi/8: e^{-i k pi/8}
         constexpr float c = (k16 == 1 || k16 == 15) ? C1 : (k16 == 3 || k16 == 13) ? S1
@@ -284,7 +296,8 @@ struct LineFft {
     static constexpr int P = num_passes(N, MB);
 
     // Tw: const float2 * (the global tables) or SmemTw<N, MB> (a copy in
-    // shared memory)
+    // shared memory).  When run() returns, other threads may still be
+    // reading the exchange buffer: sync before writing it again.
     template <class Sm, class Tw>
     __device__ __forceinline__ static void run(float2 (&x)[E], int t, Sm sm, Tw tw) {
         pass<0>(x, t, sm, tw);
@@ -353,7 +366,9 @@ struct LineFft {
 #pragma unroll
                     for (int m = 0; m < E; m++) x[m] = *sm.at(t + m * T);
                 }
-                sync();
+                // the next exchange overwrites the buffer; after the last one
+                // the caller syncs before it writes the buffer again
+                if constexpr (p + 2 < P) sync();
                 pass<p + 1>(x, t, sm, tw);
             }
         }

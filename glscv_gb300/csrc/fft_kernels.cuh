@@ -222,7 +222,11 @@ __global__ void __launch_bounds__(W *LineFft<N, E>::T)
         const size_t i = (size_t)(t + m * T) * cols + col;
         x[m] = active ? __ldg(f1 + i) : make_float2(0.f, 0.f);
     }
-    if (!(a.flags & PF_F1_SPECTRUM)) F::run(x, t, sm, a.tw);
+    __syncthreads();  // the exchange buffer is reused by the next line FFT
+    if (!(a.flags & PF_F1_SPECTRUM)) {
+        F::run(x, t, sm, a.tw);
+        __syncthreads();
+    }
 #pragma unroll
     for (int m = 0; m < E; m++) {
         const float2 s0 = x[m], s1 = y[m];

@@ -245,8 +245,9 @@ GLSFFT_API int glsfft_batch_get_schedule(glsfft_batch plan, int *schedule4);
  * Autotuner of a batch plan (no reference counterpart).  First the images
  * that get their own pass launches have their per-size pass schedules tuned
  * (glsfft_autotune_fft2d).  Then every persistent-kernel schedule -- variant
- * (GLSFFT_BATCH_*) x item-order lag (1, 2, 4, 8 resident grids) x claim
- * chunk and claim-ahead ((1, 2, 4) x (0, 1), and 1 x 2), 88 in all -- is timed, `reps` graph launches
+ * (GLSFFT_BATCH_*) x item-order lag (2, 3, 4, 5, 6, 8 resident grids) x
+ * claim chunk and claim-ahead ((1, 2, 4) x (0, 1), and 1 x 2), 132 in all --
+ * is timed, `reps` graph launches
  * each (median, CUDA events on `stream`), on a shadow plan of the same
  * shapes, flags, alignments and aliasing over scratch buffers, so the
  * plan's own images are never read or written.  The fastest is applied to

@@ -142,7 +142,7 @@ def test_batch_autotune_leaves_images_untouched_and_caches(tctx, torch_cuda, ora
         assert np.array_equal(d_in[i].cpu().numpy(), before_in[i])
         assert not d_out[i].cpu().numpy().any()
     assert not res["from_cache"]
-    assert res["candidates"] == 3 * 4 * 7 + 4  # WS1-3: 4 lags x (3 chunks x 2 + deep); plain: 4
+    assert res["candidates"] == 3 * 6 * 7 + 6  # WS1-3: 6 lags x (3 chunks x 2 + deep); plain: 6
     assert res["variant"] in (0, 1, 2, 3) and 1 <= res["claim_chunk"] <= 4
     assert b.schedule()["variant"] == res["variant"]
     assert b.schedule()["lag_items"] == res["lag_items"]
