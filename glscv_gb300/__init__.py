@@ -46,6 +46,7 @@ _SIGNATURES = {
     "glsfft_fft_cols": (_ip, [_vp, _vp, _vp, _ip, _ip, _ip, _ip, _vp]),
     "glsfft_fft2d_batched": (_ip, [_vp, _vp, _vp, _ip, _ip, _ip, _ip, _vp]),
     "glsfft_fft2d_tc": (_ip, [_vp, _vp, _vp, _ip, _ip, _ip, _ip, _vp]),
+    "glsfft_fft2d_host": (_ip, [_vp, _vp, _vp, _ip, _ip, _ip, _ip, ctypes.POINTER(_ip), _ip, _vp]),
     "glsfft_phase_correlate": (_ip, [_vp, _vp, _vp, _vp, _ip, _ip, _ip, _dp, _dp, _dp, _vp]),
     "glsfft_phase_correlate_async": (_ip, [_vp, _vp, _vp, _vp, _ip, _ip, _ip, _vp, _vp]),
     "glsfft_phase_correlate_surface": (_ip, [_vp, _vp, _sz, _vp]),
@@ -193,6 +194,14 @@ class Context:
 
     def set_budget(self, nbytes: int) -> None:
         check(lib().glsfft_context_set_budget(self.handle, nbytes), "set_budget")
+
+    def fft2d_host(self, host_src: int, host_dst: int, count: int, rows: int, cols: int,
+                   flags=(0,), chunk: int = 0, stream: int = 0) -> None:
+        """glsfft_fft2d_host: host images through 1-2 transforms, copies
+        pipelined against the transforms (asynchronous on `stream`)."""
+        fl = (_ip * len(flags))(*[int(f) for f in flags])
+        check(lib().glsfft_fft2d_host(self.handle, host_src, host_dst, count, rows, cols,
+                                      len(flags), fl, chunk, stream), "fft2d_host")
 
     def set_fft_schedule(self, rows: int, cols: int, row_schedule: int, col_schedule: int) -> None:
         check(lib().glsfft_set_fft_schedule(self.handle, rows, cols, row_schedule, col_schedule),

@@ -355,6 +355,7 @@ int glsfft_context_create(glsfft_context *out, int device) {
 int glsfft_context_destroy(glsfft_context ctx) {
     if (!ctx) return GLSFFT_ERROR_INVALID_VALUE;
     DeviceGuard g(ctx->device);
+    host_pipe_destroy(ctx->host_pipe);  // its batch plans use the context
     if (ctx->ws) cudaFree(ctx->ws);
     if (ctx->d_tw) cudaFree(ctx->d_tw);
     if (ctx->h_result) cudaFreeHost(ctx->h_result);

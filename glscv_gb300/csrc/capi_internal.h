@@ -12,6 +12,8 @@
 #include "sched_internal.h"
 #include "tc_internal.h"
 
+struct HostPipe;  // transfer.cpp: host-buffer pipeline (streams, device slots, plans)
+
 struct glsfft_context_s {
     int device = 0;
     float2 *d_tw = nullptr;     // twiddle tables, see make_twiddle_host
@@ -25,6 +27,7 @@ struct glsfft_context_s {
     // per image size (sched_key): the pass schedules the complex 2-D FFT
     // launches use; sizes not listed run schedule 0
     std::map<long long, glsfft::FftSchedule> sched;
+    HostPipe *host_pipe = nullptr;  // glsfft_fft2d_host's pipeline, built on first use
 };
 
 namespace glsfft {
@@ -54,6 +57,8 @@ constexpr int kMaxBatch = 65535;  // grid y extent
 int poc_launch(const float2 *tw, const float *src1, const float *src2, const float *window,
                int rows, int cols, int box, float2 *f1, float2 *f2, float *surface,
                unsigned long long *key, double *d_result, cudaStream_t s);
+
+void host_pipe_destroy(HostPipe *p);  // waits for its streams, frees everything
 
 // ------------------------------------------------------------- autotuner
 // The fields that identify the device a tuning was measured on.

@@ -171,6 +171,27 @@ GLSFFT_API int glsfft_autotune_fft2d(glsfft_context ctx, int rows, int cols, int
                                      const char *cache_path, void *stream, int *result,
                                      double *ms);
 
+/*
+ * gls::fft over images in host memory -- the GlsMat upload, transform,
+ * download sequence (glsCV/glsMat.cpp:374-417, :493-551 and gls::fft) for
+ * `count` rows x cols CV_32FC2 images stored back to back at host_src, each
+ * run through n_transforms (1 or 2) transforms with flags[k] (like a batch
+ * plan), results to host_dst (may equal host_src).  The images move in
+ * chunks of `chunk` images (0: automatic, about 32 MiB and at least four
+ * chunks): host -> device, a batch plan, device -> host, on three streams
+ * over a ring of three device slots, so the copies in both directions
+ * overlap the transforms.  Asynchronous: it runs after the work already
+ * queued on `stream`, and `stream` waits for the last result; synchronise it
+ * before reading host_dst.  The copies overlap only with page-locked host
+ * memory (cudaHostAlloc / cudaHostRegister).  The streams, the 3 x chunk
+ * device images and the plans stay in the context (counted against its
+ * budget) until the shape, chunk or flags change.  No reference counterpart
+ * as one call (glsCV uploads and downloads synchronously).
+ */
+GLSFFT_API int glsfft_fft2d_host(glsfft_context ctx, const void *host_src, void *host_dst,
+                                 int count, int rows, int cols, int n_transforms,
+                                 const int *flags, int chunk, void *stream);
+
 typedef struct glsfft_batch_s *glsfft_batch;
 
 /*

@@ -98,3 +98,17 @@ def test_python_binding_raises_without_device():
         pytest.skip("a GPU is present")
     with pytest.raises(g.GlsError):
         g.Context(0)
+
+
+def test_host_pipeline_and_schedule_calls_reject_bad_arguments(native):
+    fl = (ctypes.c_int * 2)(0, 3)
+    assert native.glsfft_fft2d_host(None, FAKE, FAKE, 4, 64, 64, 2, fl, 0, None) == INVALID
+    assert native.glsfft_fft2d_host(None, None, FAKE, 4, 64, 64, 2, fl, 0, None) == INVALID
+    assert native.glsfft_fft2d_host(None, FAKE, FAKE, 0, 64, 64, 2, fl, 0, None) == INVALID
+    assert native.glsfft_set_fft_schedule(None, 64, 64, 0, 0) == INVALID
+    assert native.glsfft_autotune_fft2d(None, 64, 64, 1, None, None, None, None) == INVALID
+    assert native.glsfft_batch_autotune(None, None, 5, None, None, None) == INVALID
+    assert native.glsfft_schedule_available(1024, 0, 0) == 1
+    assert native.glsfft_schedule_available(1024, 5, 0) == 0
+    assert native.glsfft_schedule_available(1000, 0, 0) == 0
+    assert native.glsfft_schedule_available(16, 1, 1) == 0
