@@ -422,6 +422,81 @@ def uneven_batch(g, ctx, torch, s, no_autotune: bool, n_images: int = 512, reps:
     return out
 
 
+def spectrum_ops(ctx, torch, s) -> dict:
+    """The spectrum operations, minMaxLoc, normalize and the FFT display
+    pipeline on 4096x4096 images (134 MB complex, larger than L2), CUDA
+    events, median of 5; achieved GB/s from the algorithmic bytes per pixel,
+    against the measured HBM copy peak.  Display latency also at 1024^2."""
+    import numpy as np
+    from glscv_gb300 import workloads as wl
+    n = 4096
+    peak, peak_kind = measured_peaks()
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(8)
+    a = torch.empty((n, n), dtype=torch.complex64, device="cuda")
+    b = torch.empty_like(a)
+    a.view(torch.float32).uniform_(-1, 1, generator=gen)
+    b.view(torch.float32).uniform_(-1, 1, generator=gen)
+    c = torch.empty_like(a)
+    f = torch.empty((n, n), dtype=torch.float32, device="cuda")
+    f2 = torch.empty_like(f)
+    w = torch.from_numpy(wl.hann_window(n, n)).cuda()
+    stream = torch.cuda.current_stream()
+
+    def med(fn, k=5):
+        fn()
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(k):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        ts.sort()
+        return ts[len(ts) // 2]
+
+    keys = torch.zeros(2, dtype=torch.int64, device="cuda")
+    ops = {
+        "mul_spectrums_conj": (24, lambda: ctx.mul_spectrums(a.data_ptr(), b.data_ptr(), c.data_ptr(), n, n, True, s)),
+        "mul_spectrums_phase_only": (24, lambda: ctx.mul_spectrums_phase_only(a.data_ptr(), b.data_ptr(), c.data_ptr(), n, n, s)),
+        "mag_spectrums": (12, lambda: ctx.mag_spectrums(a.data_ptr(), f.data_ptr(), n, n, s)),
+        "log_mag_spectrums": (12, lambda: ctx.log_mag_spectrums(a.data_ptr(), f.data_ptr(), n, n, 1.0, s)),
+        "min_max_loc_async": (4, lambda: g_lib().glsfft_min_max_loc_async(ctx.handle, f.data_ptr(), n, n, keys.data_ptr(), s)),
+        "normalize_minmax": (12, lambda: ctx.normalize_minmax(f.data_ptr(), f2.data_ptr(), n, n, 0.0, 1.0, s)),
+        "fft_display": (36, lambda: ctx.fft_display(f.data_ptr(), w.data_ptr(), f2.data_ptr(), n, n, 1.0, s)),
+    }
+    out = {"shape": f"{n}x{n}", "peak_gbs": peak, "peak_kind": peak_kind, "ops": {}}
+    for name, (bpp, fn) in ops.items():
+        ms = med(fn)
+        gbs = bpp * n * n / (ms * 1e-3) / 1e9
+        out["ops"][name] = {"ms": round(ms, 4), "bytes_per_px": bpp, "gbs": round(gbs, 1),
+                            "frac": round(gbs / peak, 4)}
+    # the display pipeline on a 1024^2 camera frame: one call at a time
+    fr = torch.from_numpy(wl.smooth_field(1024, 1024, seed=9)).cuda()
+    w1 = torch.from_numpy(wl.hann_window(1024, 1024)).cuda()
+    o1 = torch.empty_like(fr)
+    lat = []
+    for it in range(120):
+        t0 = time.perf_counter()
+        ctx.fft_display(fr.data_ptr(), w1.data_ptr(), o1.data_ptr(), 1024, 1024, 1.0, s)
+        torch.cuda.synchronize()
+        if it >= 20:
+            lat.append(time.perf_counter() - t0)
+    lat.sort()
+    out["fft_display_1024"] = {"p50_ms": round(lat[len(lat) // 2] * 1e3, 4),
+                               "p99_ms": round(lat[int(len(lat) * 0.99) - 1] * 1e3, 4),
+                               "note": "one call + stream sync at a time, host wall clock"}
+    return out
+
+
+def g_lib():
+    import glscv_gb300
+    return glscv_gb300.lib()
+
+
 def run_own(args) -> None:
     import numpy as np
     import torch
@@ -638,6 +713,7 @@ def run_own(args) -> None:
         serving = None if args.no_serving else serving_sweep(g, ctx, torch)
         precision = precision_form(ctx, torch, s)
         uneven = None if args.no_uneven else uneven_batch(g, ctx, torch, s, args.no_autotune)
+        spectrum = spectrum_ops(ctx, torch, s)
         line = {
             "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": round(ms, 4),
@@ -664,6 +740,7 @@ def run_own(args) -> None:
             "serving": serving,
             "precision_form": precision,
             "uneven_batch": uneven,
+            "spectrum_ops": spectrum,
             "clocks": clk,
             "gpu_launches": launches_per_step * args.steps,
         }

@@ -47,6 +47,16 @@ _SIGNATURES = {
     "glsfft_fft2d_batched": (_ip, [_vp, _vp, _vp, _ip, _ip, _ip, _ip, _vp]),
     "glsfft_fft2d_tc": (_ip, [_vp, _vp, _vp, _ip, _ip, _ip, _ip, _vp]),
     "glsfft_fft2d_host": (_ip, [_vp, _vp, _vp, _ip, _ip, _ip, _ip, ctypes.POINTER(_ip), _ip, _vp]),
+    "glsfft_mul_spectrums": (_ip, [_vp, _vp, _vp, _vp, _ip, _ip, _ip, _vp]),
+    "glsfft_mul_spectrums_phase_only": (_ip, [_vp, _vp, _vp, _vp, _ip, _ip, _vp]),
+    "glsfft_mag_spectrums": (_ip, [_vp, _vp, _vp, _ip, _ip, _vp]),
+    "glsfft_log_mag_spectrums": (_ip, [_vp, _vp, _vp, _ip, _ip, ctypes.c_float, _vp]),
+    "glsfft_min_max_loc": (_ip, [_vp, _vp, _ip, _ip, _dp, _dp, ctypes.POINTER(_ip),
+                                 ctypes.POINTER(_ip), _vp]),
+    "glsfft_min_max_loc_async": (_ip, [_vp, _vp, _ip, _ip, _vp, _vp]),
+    "glsfft_normalize_minmax": (_ip, [_vp, _vp, _vp, _ip, _ip, ctypes.c_double, ctypes.c_double,
+                                      _vp]),
+    "glsfft_fft_display": (_ip, [_vp, _vp, _vp, _vp, _ip, _ip, ctypes.c_float, _vp]),
     "glsfft_phase_correlate": (_ip, [_vp, _vp, _vp, _vp, _ip, _ip, _ip, _dp, _dp, _dp, _vp]),
     "glsfft_phase_correlate_async": (_ip, [_vp, _vp, _vp, _vp, _ip, _ip, _ip, _vp, _vp]),
     "glsfft_phase_correlate_surface": (_ip, [_vp, _vp, _sz, _vp]),
@@ -202,6 +212,44 @@ class Context:
         fl = (_ip * len(flags))(*[int(f) for f in flags])
         check(lib().glsfft_fft2d_host(self.handle, host_src, host_dst, count, rows, cols,
                                       len(flags), fl, chunk, stream), "fft2d_host")
+
+    # ---- spectrum operations, minMaxLoc, normalize, the FFT display pipeline
+    def mul_spectrums(self, src0: int, src1: int, dst: int, rows: int, cols: int,
+                      conj: bool = False, stream: int = 0) -> None:
+        check(lib().glsfft_mul_spectrums(self.handle, src0, src1, dst, rows, cols, int(conj),
+                                         stream), "mul_spectrums")
+
+    def mul_spectrums_phase_only(self, src0: int, src1: int, dst: int, rows: int, cols: int,
+                                 stream: int = 0) -> None:
+        check(lib().glsfft_mul_spectrums_phase_only(self.handle, src0, src1, dst, rows, cols,
+                                                    stream), "mul_spectrums_phase_only")
+
+    def mag_spectrums(self, src: int, dst: int, rows: int, cols: int, stream: int = 0) -> None:
+        check(lib().glsfft_mag_spectrums(self.handle, src, dst, rows, cols, stream),
+              "mag_spectrums")
+
+    def log_mag_spectrums(self, src: int, dst: int, rows: int, cols: int, offset: float,
+                          stream: int = 0) -> None:
+        check(lib().glsfft_log_mag_spectrums(self.handle, src, dst, rows, cols, offset, stream),
+              "log_mag_spectrums")
+
+    def min_max_loc(self, src: int, rows: int, cols: int, stream: int = 0):
+        """((min, max), (min_x, min_y), (max_x, max_y)), synchronous."""
+        mn, mx = ctypes.c_double(), ctypes.c_double()
+        lmin, lmax = (_ip * 2)(), (_ip * 2)()
+        check(lib().glsfft_min_max_loc(self.handle, src, rows, cols, ctypes.byref(mn),
+                                       ctypes.byref(mx), lmin, lmax, stream), "min_max_loc")
+        return (mn.value, mx.value), (lmin[0], lmin[1]), (lmax[0], lmax[1])
+
+    def normalize_minmax(self, src: int, dst: int, rows: int, cols: int, alpha: float = 0.0,
+                         beta: float = 1.0, stream: int = 0) -> None:
+        check(lib().glsfft_normalize_minmax(self.handle, src, dst, rows, cols, alpha, beta,
+                                            stream), "normalize_minmax")
+
+    def fft_display(self, frame: int, window: int | None, dst: int, rows: int, cols: int,
+                    offset: float = 1.0, stream: int = 0) -> None:
+        check(lib().glsfft_fft_display(self.handle, frame, window, dst, rows, cols, offset,
+                                       stream), "fft_display")
 
     def set_fft_schedule(self, rows: int, cols: int, row_schedule: int, col_schedule: int) -> None:
         check(lib().glsfft_set_fft_schedule(self.handle, rows, cols, row_schedule, col_schedule),

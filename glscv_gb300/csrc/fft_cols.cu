@@ -41,6 +41,7 @@ static cudaError_t cols_n(int n, const PassArgs &a, int images, cudaStream_t s) 
 
 cudaError_t launch_cols(int n, int ld, int st, const PassArgs &a, int images, cudaStream_t s) {
     if (ld == LD_C2 && st == ST_C2) return cols_n<LD_C2, ST_C2>(n, a, images, s);
+    if (ld == LD_C2 && st == ST_LOGMAG_MINMAX) return cols_n<LD_C2, ST_LOGMAG_MINMAX>(n, a, images, s);
     return cudaErrorInvalidValue;
 }
 

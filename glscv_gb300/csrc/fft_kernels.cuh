@@ -16,6 +16,7 @@
 #include "fft_config.h"
 #include "fft_device.cuh"
 #include "glsfft_internal.h"
+#include "spectrum_device.cuh"
 
 namespace glsfft {
 
@@ -179,10 +180,33 @@ __global__ void __launch_bounds__(W *LineFft<N, E>::T)
 
     const int ocol = (a.flags & PF_SHIFT_COLS) ? (col + (cols >> 1)) & (cols - 1) : col;
     finish_line(x, a.scale, a.flags & PF_CONJ_OUT);
-    static_assert(ST == ST_C2, "the column pass stores complex values");
-    if (active)
-        store_line<N, E, T>(reinterpret_cast<float2 *>(out) + ocol, (size_t)cols, x, t,
-                            a.flags & PF_SHIFT_ROWS);
+    if constexpr (ST == ST_C2) {
+        if (active)
+            store_line<N, E, T>(reinterpret_cast<float2 *>(out) + ocol, (size_t)cols, x, t,
+                                a.flags & PF_SHIFT_ROWS);
+    } else {
+        // the FFT display epilogue: log(|magnitude| + offset) as CV_32FC1
+        // (glsBasicOperation.cpp:126-128) and the minMaxLoc keys of what is
+        // stored, for the normalisation that follows
+        static_assert(ST == ST_LOGMAG_MINMAX, "column-pass store variants: complex, log-magnitude");
+        __shared__ unsigned long long red[2 * ((W * T + 31) / 32)];
+        unsigned long long kmin = 0, kmax = 0;
+        float *fo = reinterpret_cast<float *>(out);
+#pragma unroll
+        for (int m = 0; m < E; m++) {
+            const int pos = t + m * T;
+            const int orow = (a.flags & PF_SHIFT_ROWS) ? (pos + (N >> 1)) & (N - 1) : pos;
+            const unsigned o = (unsigned)orow * (unsigned)cols + (unsigned)ocol;
+            const float v = spec_log_mag(x[m], a.param);
+            if (active) {
+                fo[o] = v;
+                const unsigned long long k0 = min_key(v, o), k1 = max_key(v, o);
+                kmin = k0 > kmin ? k0 : kmin;
+                kmax = k1 > kmax ? k1 : kmax;
+            }
+        }
+        block_minmax_commit(kmin, kmax, red, a.key);
+    }
 }
 
 // --------------------------------------------- fused phaseCorrelate columns

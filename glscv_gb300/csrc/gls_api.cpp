@@ -159,4 +159,82 @@ Point2d phaseCorrelate(const GlsMat &src1, const GlsMat &src2, GlsMat &window, d
     return phaseCorrelate(src1, src2, window, response, 5);
 }
 
+// ------------------------------------------------------ spectrum operations
+namespace {
+// getDstMat (glsMat.h:173-213): dst keeps its storage when it already has
+// the size and type, else it gets a new image
+void dst_for(GlsMat &dst, Size size, int type) {
+    if (dst.empty() || dst.size() != size || dst.type() != type) dst = GlsMat(size, type);
+}
+void check_spectrum(const GlsMat &m, const char *where) {
+    assert_that(!m.empty() && m.type() == CV_32FC2, where);
+}
+}  // namespace
+
+void mulSpectrums(const GlsMat &src0, const GlsMat &src1, GlsMat &dst, bool conj) {
+    // glsBasicOperation.cpp:320-326
+    check_spectrum(src0, "gls::mulSpectrums: src0 must be CV_32FC2");
+    check_spectrum(src1, "gls::mulSpectrums: src1 must be CV_32FC2");
+    if (src0.size() != src1.size()) throw Exception(GLSFFT_ERROR_SHAPE, "gls::mulSpectrums");
+    dst_for(dst, src0.size(), CV_32FC2);
+    check(glsfft_mul_spectrums(context(), src0.devptr(), src1.devptr(), dst.devptr(), src0.rows,
+                               src0.cols, conj ? 1 : 0, nullptr),
+          "gls::mulSpectrums");
+}
+
+void mulSpectrumsPhaseOnly(const GlsMat &src0, const GlsMat &src1, GlsMat &dst) {
+    // glsBasicOperation.cpp:329-335
+    check_spectrum(src0, "gls::mulSpectrumsPhaseOnly: src0 must be CV_32FC2");
+    check_spectrum(src1, "gls::mulSpectrumsPhaseOnly: src1 must be CV_32FC2");
+    if (src0.size() != src1.size()) throw Exception(GLSFFT_ERROR_SHAPE, "gls::mulSpectrumsPhaseOnly");
+    dst_for(dst, src0.size(), CV_32FC2);
+    check(glsfft_mul_spectrums_phase_only(context(), src0.devptr(), src1.devptr(), dst.devptr(),
+                                          src0.rows, src0.cols, nullptr),
+          "gls::mulSpectrumsPhaseOnly");
+}
+
+void magSpectrums(const GlsMat &src, GlsMat &dst) {
+    // glsBasicOperation.cpp:337-343
+    check_spectrum(src, "gls::magSpectrums: src must be CV_32FC2");
+    if (dst.shares(src)) dst = GlsMat();
+    dst_for(dst, src.size(), CV_32FC1);
+    check(glsfft_mag_spectrums(context(), src.devptr(), static_cast<float *>(dst.devptr()),
+                               src.rows, src.cols, nullptr),
+          "gls::magSpectrums");
+}
+
+void logMagSpectrums(const GlsMat &src, GlsMat &dst, float offset) {
+    // glsBasicOperation.cpp:345-351
+    check_spectrum(src, "gls::logMagSpectrums: src must be CV_32FC2");
+    if (dst.shares(src)) dst = GlsMat();
+    dst_for(dst, src.size(), CV_32FC1);
+    check(glsfft_log_mag_spectrums(context(), src.devptr(), static_cast<float *>(dst.devptr()),
+                                   src.rows, src.cols, offset, nullptr),
+          "gls::logMagSpectrums");
+}
+
+void minMaxLoc(const GlsMat &src, double *minVal, double *maxVal, Point *minLoc, Point *maxLoc,
+               const GlsMat &mask) {
+    // glsMinMaxLoc.cpp:149-153
+    assert_that(!src.empty() && src.type() == CV_32FC1, "gls::minMaxLoc: src must be CV_32FC1");
+    assert_that(mask.empty(), "gls::minMaxLoc: masks are not implemented (as in the reference)");
+    int lmin[2] = {0, 0}, lmax[2] = {0, 0};
+    check(glsfft_min_max_loc(context(), static_cast<const float *>(src.devptr()), src.rows,
+                             src.cols, minVal, maxVal, lmin, lmax, nullptr),
+          "gls::minMaxLoc");
+    if (minLoc) *minLoc = Point(lmin[0], lmin[1]);
+    if (maxLoc) *maxLoc = Point(lmax[0], lmax[1]);
+}
+
+void normalize(const GlsMat &src, GlsMat &dst, double alpha, double beta, int normType) {
+    // glsNormalize.cpp:52-68
+    assert_that(!src.empty() && src.type() == CV_32FC1, "gls::normalize: src must be CV_32FC1");
+    assert_that(normType == NORM_MINMAX, "gls::normalize: only NORM_MINMAX is implemented");
+    dst_for(dst, src.size(), CV_32FC1);
+    check(glsfft_normalize_minmax(context(), static_cast<const float *>(src.devptr()),
+                                  static_cast<float *>(dst.devptr()), src.rows, src.cols, alpha,
+                                  beta, nullptr),
+          "gls::normalize");
+}
+
 }  // namespace gls

@@ -25,7 +25,9 @@ __host__ __device__ constexpr int tw_offset(int r, int l) {
 // load modes of the first pass
 enum { LD_C2 = 0, LD_R1 = 1, LD_R1W = 2 };
 // store modes of the last pass
-enum { ST_C2 = 0, ST_RE = 1, ST_RE_ARGMAX = 2 };
+// ST_LOGMAG_MINMAX: log(|sqrt(re^2 + im^2) + param|) stored as CV_32FC1, with
+// the minMaxLoc keys of the stored values reduced into key[0] (min), key[1] (max)
+enum { ST_C2 = 0, ST_RE = 1, ST_RE_ARGMAX = 2, ST_LOGMAG_MINMAX = 3 };
 // per-pass flags
 enum : unsigned {
     PF_CONJ_IN = 1u << 0,
@@ -48,6 +50,7 @@ struct PassArgs {
     const float2 *tw;  // twiddle table of this pass's length
     size_t in_img_bytes;   // batch: byte stride between images (0 = single / in1 mode)
     size_t out_img_bytes;
+    float param;       // ST_LOGMAG_MINMAX: the log-magnitude offset
 };
 
 // Launchers (fft_rows.cu, fft_cols.cu, poc.cu).  They return cudaSuccess or

@@ -35,6 +35,7 @@ enum { CV_32F = 5, CV_32FC1 = 5, CV_32FC2 = 13 };
 enum { DFT_INVERSE = 1, DFT_SCALE = 2 };
 // glsCV/glsFft.h:43-47
 enum { GLS_FFT_SCALE = DFT_SCALE, GLS_FFT_INVERSE = DFT_INVERSE, GLS_FFT_SHIFT = 64 };
+enum { NORM_INF = 1, NORM_L1 = 2, NORM_L2 = 4, NORM_MINMAX = 32 };  // OpenCV values
 
 inline int cv_depth(int type) { return type & 7; }
 inline int cv_channels(int type) { return (type >> 3) + 1; }
@@ -151,6 +152,24 @@ GLS_EXPORT Point2d phaseCorrelate(const GlsMat &src1, const GlsMat &src2, GlsMat
 // Same with an explicit centroid box (the reference fixes 5, :219).
 GLS_EXPORT Point2d phaseCorrelate(const GlsMat &src1, const GlsMat &src2, GlsMat &window,
                                   double *response, int box);
+
+// glsCV/glsBasicOperation.h:78-88: CV_32FC2 spectra; dst is (re)allocated
+// like getDstMat does (CV_32FC2 for the products, CV_32FC1 for magnitudes).
+GLS_EXPORT void mulSpectrums(const GlsMat &src0, const GlsMat &src1, GlsMat &dst,
+                             bool conj = false);
+GLS_EXPORT void mulSpectrumsPhaseOnly(const GlsMat &src0, const GlsMat &src1, GlsMat &dst);
+GLS_EXPORT void magSpectrums(const GlsMat &src, GlsMat &dst);
+GLS_EXPORT void logMagSpectrums(const GlsMat &src, GlsMat &dst, float offset);
+
+// glsCV/glsMinMaxLoc.h:42: CV_32FC1; first occurrence in row-major order.
+// The mask must be empty, as in the reference (glsMinMaxLoc.cpp:153).
+GLS_EXPORT void minMaxLoc(const GlsMat &src, double *minVal, double *maxVal = 0,
+                          Point *minLoc = 0, Point *maxLoc = 0, const GlsMat &mask = GlsMat());
+
+// glsCV/glsNormalize.h:47: CV_32FC1.  NORM_MINMAX (dst in [alpha, beta]) is
+// implemented; NORM_L1 / NORM_L2 throw (they need gls::norm, outside this path).
+GLS_EXPORT void normalize(const GlsMat &src, GlsMat &dst, double alpha = 1, double beta = 0,
+                          int normType = NORM_L2);
 
 }  // namespace gls
 

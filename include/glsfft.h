@@ -192,6 +192,68 @@ GLSFFT_API int glsfft_fft2d_host(glsfft_context ctx, const void *host_src, void 
                                  int count, int rows, int cols, int n_transforms,
                                  const int *flags, int chunk, void *stream);
 
+/*
+ * Spectrum operations on rows x cols device images (any size; the CV_32FC2
+ * results may be written in place, the CV_32FC1 ones must not overlap their
+ * input), element formulas of the reference shaders with every product, sum
+ * and quotient rounded separately:
+ *   glsfft_mul_spectrums            gls::mulSpectrums(src0, src1, dst, conj)
+ *                                   (glsCV/glsBasicOperation.cpp:320-326): a*b or
+ *                                   a*conj(b), CV_32FC2
+ *   glsfft_mul_spectrums_phase_only gls::mulSpectrumsPhaseOnly (:329-335):
+ *                                   t = a*conj(b), t/|t| (0/0 is NaN, as there)
+ *   glsfft_mag_spectrums            gls::magSpectrums (:337-343): |a| as CV_32FC1
+ *   glsfft_log_mag_spectrums        gls::logMagSpectrums(src, dst, offset)
+ *                                   (:345-351): log(| |a| + offset |) as CV_32FC1
+ */
+GLSFFT_API int glsfft_mul_spectrums(glsfft_context ctx, const void *src0, const void *src1,
+                                    void *dst, int rows, int cols, int conj, void *stream);
+GLSFFT_API int glsfft_mul_spectrums_phase_only(glsfft_context ctx, const void *src0,
+                                               const void *src1, void *dst, int rows, int cols,
+                                               void *stream);
+GLSFFT_API int glsfft_mag_spectrums(glsfft_context ctx, const void *src, float *dst, int rows,
+                                    int cols, void *stream);
+GLSFFT_API int glsfft_log_mag_spectrums(glsfft_context ctx, const void *src, float *dst,
+                                        int rows, int cols, float offset, void *stream);
+
+/*
+ * gls::minMaxLoc(src, &minVal, &maxVal, &minLoc, &maxLoc) on a CV_32FC1 device
+ * image (glsCV/glsMinMaxLoc.cpp:149-200): the first occurrence in row-major
+ * order of the smallest and largest values; as in the reference shader only
+ * values below (above) its FLT_MAX literal 3.402823e+38 take part and NaN
+ * never does, and with none the literal is returned at (0, 0).  Locations are
+ * {x, y}; any output may be NULL.  Synchronises `stream`.
+ * glsfft_min_max_loc_async leaves the two 64-bit keys in d_keys instead
+ * (min, max: order-preserving value bits << 32 | 0xFFFFFFFF - (y*cols + x),
+ * 0 = none).
+ */
+GLSFFT_API int glsfft_min_max_loc(glsfft_context ctx, const float *src, int rows, int cols,
+                                  double *min_val, double *max_val, int *min_loc, int *max_loc,
+                                  void *stream);
+GLSFFT_API int glsfft_min_max_loc_async(glsfft_context ctx, const float *src, int rows,
+                                        int cols, unsigned long long *d_keys, void *stream);
+
+/*
+ * gls::normalize(src, dst, alpha, beta, NORM_MINMAX) on a CV_32FC1 device
+ * image (glsCV/glsNormalize.cpp:52-68): scl = (float)(beta - alpha) /
+ * (float)(max - min), dst = (float)(alpha - scl*min) + scl*src; the min / max
+ * stay on the device (asynchronous).
+ */
+GLSFFT_API int glsfft_normalize_minmax(glsfft_context ctx, const float *src, float *dst,
+                                       int rows, int cols, double alpha, double beta,
+                                       void *stream);
+
+/*
+ * glsCam's FFT view as one pipeline on device buffers (glsCam/glsCam.cpp:196-203):
+ * window * frame (CV_32FC1; window may be NULL), gls::fft with GLS_FFT_SHIFT,
+ * logMagSpectrums(offset), normalize(0, 1, NORM_MINMAX) -> dst (CV_32FC1).
+ * The log-magnitude and its min / max are fused into the column FFT; the
+ * camera, colour conversion and drawing are left out.  Powers of two;
+ * asynchronous.
+ */
+GLSFFT_API int glsfft_fft_display(glsfft_context ctx, const float *frame, const float *window,
+                                  float *dst, int rows, int cols, float offset, void *stream);
+
 typedef struct glsfft_batch_s *glsfft_batch;
 
 /*

@@ -73,6 +73,12 @@ def lib():
             ctypes.c_int, _dp, _dp, _dp, _f32p, _ip]
         l.oracle_max_loc.argtypes = [_f32p, ctypes.c_int, ctypes.c_int, _ip, _ip, _f32p]
         l.oracle_mul_spectrums.argtypes = [_f32p, _f32p, _f32p, ctypes.c_size_t, ctypes.c_int]
+        l.oracle_mul_spectrums_poc.argtypes = [_f32p, _f32p, _f32p, ctypes.c_size_t]
+        l.oracle_mag_spectrums.argtypes = [_f32p, _f32p, ctypes.c_size_t, ctypes.c_int,
+                                           ctypes.c_float]
+        l.oracle_min_max_loc.argtypes = [_f32p, ctypes.c_int, ctypes.c_int, _dp, _dp, _ip, _ip]
+        l.oracle_normalize_minmax.argtypes = [_f32p, _f32p, ctypes.c_int, ctypes.c_int,
+                                              ctypes.c_double, ctypes.c_double]
         l.oracle_set_threads.argtypes = [ctypes.c_int]
         _lib = l
     return _lib
@@ -186,6 +192,50 @@ def mul_spectrums(a: np.ndarray, b: np.ndarray, conj: bool = False) -> np.ndarra
     lib().oracle_mul_spectrums(_fp(a.view(np.float32)), _fp(b.view(np.float32)),
                                _fp(out.view(np.float32)), a.size, int(conj))
     return out
+
+
+def mul_spectrums_phase_only(a: np.ndarray, b: np.ndarray) -> np.ndarray:
+    a, b = _c64(a), _c64(b)
+    out = np.empty_like(a)
+    lib().oracle_mul_spectrums_poc(_fp(a.view(np.float32)), _fp(b.view(np.float32)),
+                                   _fp(out.view(np.float32)), a.size)
+    return out
+
+
+def mag_spectrums(a: np.ndarray, log_mag: bool = False, offset: float = 0.0) -> np.ndarray:
+    a = _c64(a)
+    out = np.empty(a.shape, np.float32)
+    lib().oracle_mag_spectrums(_fp(a.view(np.float32)), _fp(out), a.size, int(log_mag),
+                               ctypes.c_float(offset))
+    return out
+
+
+def min_max_loc(x: np.ndarray):
+    """((min, max), (min_x, min_y), (max_x, max_y)) with gls::minMaxLoc semantics."""
+    x = np.ascontiguousarray(x, dtype=np.float32)
+    mn, mx = ctypes.c_double(), ctypes.c_double()
+    lmin, lmax = (ctypes.c_int * 2)(), (ctypes.c_int * 2)()
+    lib().oracle_min_max_loc(_fp(x), x.shape[0], x.shape[1], ctypes.byref(mn), ctypes.byref(mx),
+                             ctypes.cast(lmin, _ip), ctypes.cast(lmax, _ip))
+    return (mn.value, mx.value), (lmin[0], lmin[1]), (lmax[0], lmax[1])
+
+
+def normalize_minmax(x: np.ndarray, alpha: float = 0.0, beta: float = 1.0) -> np.ndarray:
+    x = np.ascontiguousarray(x, dtype=np.float32)
+    out = np.empty_like(x)
+    lib().oracle_normalize_minmax(_fp(x), _fp(out), x.shape[0], x.shape[1],
+                                  ctypes.c_double(alpha), ctypes.c_double(beta))
+    return out
+
+
+def fft_display(frame: np.ndarray, window: np.ndarray | None, offset: float = 1.0) -> np.ndarray:
+    """glsCam's FFT view (glsCam/glsCam.cpp:196-203): window * frame, gls::fft
+    with GLS_FFT_SHIFT, logMagSpectrums(offset), normalize(0, 1, NORM_MINMAX)."""
+    f = np.ascontiguousarray(frame, dtype=np.float32)
+    if window is not None:
+        f = (np.ascontiguousarray(window, dtype=np.float32) * f).astype(np.float32)
+    spec = fft2d(f.astype(np.complex64), GLS_FFT_SHIFT, 0)
+    return normalize_minmax(mag_spectrums(spec, True, offset), 0.0, 1.0)
 
 
 # ---------------------------------------------------------------- FP64 yardstick

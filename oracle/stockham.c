@@ -398,6 +398,73 @@ void oracle_mul_spectrums(const float *a, const float *b, float *out, size_t n, 
     }
 }
 
+/* mulSpectrumsPhaseOnly (glsCV/glsBasicOperation.cpp:195-206, shader op 8):
+ * t = a * conj(b), out = t / sqrt(t.re^2 + t.im^2), no epsilon (0/0 = NaN). */
+void oracle_mul_spectrums_poc(const float *a, const float *b, float *out, size_t n) {
+    for (size_t i = 0; i < n; i++) {
+        float ar = a[2 * i], ai = a[2 * i + 1], br = b[2 * i], bi = b[2 * i + 1];
+        float tr = ar * br + ai * bi, ti = -ar * bi + ai * br;
+        float mag = sqrtf(tr * tr + ti * ti);
+        out[2 * i] = tr / mag;
+        out[2 * i + 1] = ti / mag;
+    }
+}
+
+/* magSpectrums / logMagSpectrums (glsBasicOperation.cpp:117-119, :126-128,
+ * shader ops 9 and 13): sqrt(re^2 + im^2), log(|sqrt(re^2 + im^2) + offset|). */
+void oracle_mag_spectrums(const float *a, float *out, size_t n, int log_mag, float offset) {
+    for (size_t i = 0; i < n; i++) {
+        float r = a[2 * i], g = a[2 * i + 1];
+        float mag = sqrtf(r * r + g * g);
+        out[i] = log_mag ? logf(fabsf(mag + offset)) : mag;
+    }
+}
+
+/* gls::minMaxLoc (glsCV/glsMinMaxLoc.cpp:65-119, :149-200): a strict-compare
+ * scan of every row from the FLT_MAX literal of the shader, then a strict
+ * scan of the row results -- the first occurrence in row-major order; an
+ * element takes part only if it compares below (above) the literal, and
+ * when none does the result is the literal at (0, 0).  loc = {x, y}. */
+void oracle_min_max_loc(const float *x, int rows, int cols, double *min_val, double *max_val,
+                        int *min_loc, int *max_loc) {
+    const float lit = 3.402823e+38f;
+    float gmin = lit, gmax = -lit;
+    int gminx = 0, gminy = 0, gmaxx = 0, gmaxy = 0;
+    for (int y = 0; y < rows; y++) {
+        float rmin = lit, rmax = -lit;
+        int rminx = 0, rmaxx = 0;
+        for (int c = 0; c < cols; c++) {
+            float d = x[(size_t)y * cols + c];
+            if (d < rmin) { rmin = d; rminx = c; }
+            if (d > rmax) { rmax = d; rmaxx = c; }
+        }
+        if (rmin < gmin) { gmin = rmin; gminx = rminx; gminy = y; }
+        if (rmax > gmax) { gmax = rmax; gmaxx = rmaxx; gmaxy = y; }
+    }
+    /* rows that never updated report x = 0 of their own row, as the shader's
+     * second pass reads the row's stored location (0 by default) */
+    if (min_val) *min_val = gmin;
+    if (max_val) *max_val = gmax;
+    if (min_loc) { min_loc[0] = gminx; min_loc[1] = gminy; }
+    if (max_loc) { max_loc[0] = gmaxx; max_loc[1] = gmaxy; }
+}
+
+/* gls::normalize(src, dst, alpha, beta, NORM_MINMAX) (glsCV/glsNormalize.cpp:52-68):
+ * scl = (float)(beta - alpha) / (float)(max - min); dst = (float)(alpha - scl*min)
+ * + scl * src, the product and the sum each rounded to float. */
+void oracle_normalize_minmax(const float *x, float *out, int rows, int cols, double alpha,
+                             double beta) {
+    double mn, mx;
+    oracle_min_max_loc(x, rows, cols, &mn, &mx, 0, 0);
+    float scl = (float)(beta - alpha) / (float)(mx - mn);
+    float c = (float)(alpha - (double)scl * mn);
+    size_t n = (size_t)rows * cols;
+    for (size_t i = 0; i < n; i++) {
+        float t = scl * x[i];
+        out[i] = c + t;
+    }
+}
+
 int oracle_num_threads(void) {
 #ifdef _OPENMP
     return omp_get_max_threads();

@@ -173,11 +173,68 @@ static void test_errors() {
     EXPECT(thrown, "phaseCorrelate size mismatch throws");
 }
 
+// the spectrum operations, minMaxLoc and normalize, written like the
+// reference's UnitTest_glsBasicOperation / UnitTest_glsMinMaxLoc checks
+static void test_spectrum_ops() {
+    const int R = 24, C = 32;  // the reference minMaxLoc test's size
+    Mat a = random_complex(R, C, 31), b = random_complex(R, C, 32);
+    GlsMat ga(a), gb(b), prod, conj_prod, poc, mag, lmag;
+    gls::mulSpectrums(ga, gb, prod, false);
+    gls::mulSpectrums(ga, gb, conj_prod, true);
+    gls::mulSpectrumsPhaseOnly(ga, gb, poc);
+    gls::magSpectrums(ga, mag);
+    gls::logMagSpectrums(ga, lmag, 1.0f);
+    Mat hp = prod, hc = conj_prod, hpoc = poc, hm = mag, hl = lmag;
+    EXPECT(hm.type() == gls::CV_32FC1 && hl.type() == gls::CV_32FC1, "magnitudes are CV_32FC1");
+    const float *pa = a.ptr<float>(), *pb = b.ptr<float>();
+    double e_prod = 0, e_conj = 0, e_poc = 0, e_mag = 0, e_log = 0;
+    for (size_t i = 0; i < a.total(); i++) {
+        const std::complex<double> x(pa[2 * i], pa[2 * i + 1]), y(pb[2 * i], pb[2 * i + 1]);
+        const std::complex<double> p = x * y, c = x * std::conj(y), n = c / std::abs(c);
+        e_prod = std::fmax(e_prod, std::abs(p - std::complex<double>(hp.ptr<float>()[2 * i], hp.ptr<float>()[2 * i + 1])));
+        e_conj = std::fmax(e_conj, std::abs(c - std::complex<double>(hc.ptr<float>()[2 * i], hc.ptr<float>()[2 * i + 1])));
+        e_poc = std::fmax(e_poc, std::abs(n - std::complex<double>(hpoc.ptr<float>()[2 * i], hpoc.ptr<float>()[2 * i + 1])));
+        e_mag = std::fmax(e_mag, std::fabs(std::abs(x) - hm.ptr<float>()[i]));
+        e_log = std::fmax(e_log, std::fabs(std::log(std::abs(x) + 1.0) - hl.ptr<float>()[i]));
+    }
+    EXPECT(e_prod < 1e-6 && e_conj < 1e-6, "mulSpectrums matches a double product");
+    EXPECT(e_poc < 1e-6, "mulSpectrumsPhaseOnly matches");
+    EXPECT(e_mag < 1e-6 && e_log < 1e-6, "magSpectrums / logMagSpectrums match");
+
+    Mat img(R, C, gls::CV_32FC1);
+    std::mt19937 rng(33);
+    std::uniform_real_distribution<float> u(-1.f, 1.f);
+    float *pi = img.ptr<float>();
+    for (size_t i = 0; i < img.total(); i++) pi[i] = u(rng);
+    pi[5 * C + 7] = 3.f;   // maximum, once more later: the first one counts
+    pi[20 * C + 1] = 3.f;
+    pi[2 * C + 30] = -3.f;
+    GlsMat gimg(img);
+    double mn = 0, mx = 0;
+    gls::Point lmin, lmax;
+    gls::minMaxLoc(gimg, &mn, &mx, &lmin, &lmax);
+    EXPECT(mn == -3.0 && mx == 3.0, "minMaxLoc values");
+    EXPECT(lmin.x == 30 && lmin.y == 2 && lmax.x == 7 && lmax.y == 5, "minMaxLoc first occurrence");
+    GlsMat nrm;
+    gls::normalize(gimg, nrm, 0, 1, gls::NORM_MINMAX);
+    Mat hn = nrm;
+    EXPECT(hn.ptr<float>()[2 * C + 30] == 0.f && std::fabs(hn.ptr<float>()[5 * C + 7] - 1.f) < 1e-6f,
+           "normalize NORM_MINMAX maps min to 0 and max to 1");
+    bool thrown = false;
+    try {
+        gls::normalize(gimg, nrm, 1, 0, gls::NORM_L2);
+    } catch (const gls::Exception &) {
+        thrown = true;
+    }
+    EXPECT(thrown, "normalize NORM_L2 is outside this path and throws");
+}
+
 int main() {
     gls::glsCvInit(0);
     test_fft();
     test_phase_correlate();
     test_errors();
+    test_spectrum_ops();
     gls::glsCvTerminate();
     if (failures) {
         std::printf("%d FAILURES\n", failures);

@@ -132,3 +132,35 @@ def test_hann_window_shape():
     w = wl.hann_window(8, 16)
     assert w.shape == (8, 16) and w.dtype == np.float32
     assert w[0, 0] == 0.0 and abs(w[4, 8] - np.sin(np.pi * 4 / 7) ** 2 * np.sin(np.pi * 8 / 15) ** 2) < 1e-6
+
+
+# ------------------------------------------------ spectrum ops, minMaxLoc, normalize
+
+def test_min_max_loc_restatement_semantics(oracle):
+    """gls::minMaxLoc (glsMinMaxLoc.cpp:65-119): first occurrence in row-major
+    order, NaN ignored, values beyond the shader's FLT_MAX literal ignored."""
+    x = np.array([[3, 1, 2], [0, 5, -1], [5, -1, 0]], np.float32)
+    assert oracle.min_max_loc(x) == ((-1.0, 5.0), (2, 1), (1, 1))
+    x = np.array([[np.nan, 2], [2, np.nan]], np.float32)
+    assert oracle.min_max_loc(x) == ((2.0, 2.0), (1, 0), (1, 0))
+    x = np.full((2, 3), np.inf, np.float32)
+    (mn, mx), lmin, lmax = oracle.min_max_loc(x)
+    assert mn == float(np.float32(3.402823e+38)) and lmin == (0, 0)
+    assert mx == np.inf and lmax == (0, 0)
+    x = np.array([[0.0, -0.0], [-0.0, 0.0]], np.float32)  # -0 == +0: the first one wins
+    assert oracle.min_max_loc(x)[1:] == ((0, 0), (0, 0))
+
+
+def test_normalize_and_spectrum_restatements(oracle):
+    x = np.array([[1, 2], [3, 5]], np.float32)
+    assert np.array_equal(oracle.normalize_minmax(x), np.array([[0, .25], [.5, 1]], np.float32))
+    rng = np.random.default_rng(0)
+    a = (rng.standard_normal((8, 8)) + 1j * rng.standard_normal((8, 8))).astype(np.complex64)
+    b = (rng.standard_normal((8, 8)) + 1j * rng.standard_normal((8, 8))).astype(np.complex64)
+    assert np.allclose(oracle.mag_spectrums(a), np.abs(a), rtol=1e-6)
+    assert np.allclose(oracle.mag_spectrums(a, True, 1.0), np.log(np.abs(a) + 1), rtol=1e-6)
+    assert np.allclose(oracle.mul_spectrums(a, b, True), a * np.conj(b), rtol=1e-5, atol=1e-6)
+    p = oracle.mul_spectrums_phase_only(a, b)
+    assert np.allclose(np.abs(p), 1, atol=1e-6)
+    z = oracle.mul_spectrums_phase_only(np.zeros_like(a), b)
+    assert np.isnan(z.view(np.float32)).all()  # 0/0, no epsilon (glsBasicOperation.cpp:202-205)
