@@ -28,13 +28,15 @@ namespace {
 
 constexpr int kThreads = 256;
 
-int grid_for(size_t n) {
+// blocks for n elements: per_sm resident blocks per SM at most (grid-stride
+// beyond); reductions use fewer, longer blocks to keep the per-block atomics few
+int grid_for(size_t n, int per_sm = 8) {
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (sms <= 0) sms = 1;
     const size_t want = (n + kThreads - 1) / kThreads;
-    const size_t cap = (size_t)sms * 8;  // 8 resident blocks per SM, grid-stride beyond
+    const size_t cap = (size_t)sms * per_sm;
     return (int)(want < cap ? (want ? want : 1) : cap);
 }
 
@@ -125,28 +127,50 @@ __global__ void __launch_bounds__(kThreads) spec_mag_kernel(const float2 *__rest
     if constexpr (KEYS) block_minmax_commit(kmin, kmax, red, keys);
 }
 
+// Each thread visits its indices in increasing order, so a running strict
+// compare keeps its first occurrence; keys are formed once per thread for the
+// block reduction.  Starting from the literal excludes what the reference
+// excludes (NaN and values at or beyond it never compare).
+struct MinMaxRun {
+    float vmin = kMinMaxLiteral, vmax = -kMinMaxLiteral;
+    unsigned imin = 0, imax = 0;
+    __device__ __forceinline__ void add(float v, unsigned i) {
+        if (v < vmin) {
+            vmin = v;
+            imin = i;
+        }
+        if (v > vmax) {
+            vmax = v;
+            imax = i;
+        }
+    }
+    __device__ __forceinline__ void commit(unsigned long long *red, unsigned long long *keys) const {
+        block_minmax_commit(min_key(vmin, imin), max_key(vmax, imax), red, keys);
+    }
+};
+
 __global__ void __launch_bounds__(kThreads) minmax_kernel(const float *__restrict__ x, size_t n,
                                                           unsigned long long *keys) {
     __shared__ unsigned long long red[2 * (kThreads / 32)];
-    unsigned long long kmin = 0, kmax = 0;
+    MinMaxRun run;
     const size_t tid = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
     const size_t stride = (size_t)gridDim.x * blockDim.x;
     size_t done = 0;
     if (al16(x)) {
         const size_t nv = n / 4;
         const float4 *x4 = reinterpret_cast<const float4 *>(x);
-#pragma unroll 2
+#pragma unroll 4
         for (size_t i = tid; i < nv; i += stride) {
             const float4 v = x4[i];
-            keys_add(v.x, 4 * i, kmin, kmax);
-            keys_add(v.y, 4 * i + 1, kmin, kmax);
-            keys_add(v.z, 4 * i + 2, kmin, kmax);
-            keys_add(v.w, 4 * i + 3, kmin, kmax);
+            run.add(v.x, (unsigned)(4 * i));
+            run.add(v.y, (unsigned)(4 * i + 1));
+            run.add(v.z, (unsigned)(4 * i + 2));
+            run.add(v.w, (unsigned)(4 * i + 3));
         }
         done = nv * 4;
     }
-    for (size_t i = done + tid; i < n; i += stride) keys_add(x[i], i, kmin, kmax);
-    block_minmax_commit(kmin, kmax, red, keys);
+    for (size_t i = done + tid; i < n; i += stride) run.add(x[i], (unsigned)i);
+    run.commit(red, keys);
 }
 
 // dst = (float)(alpha - scl*min) + scl*src, scl = (float)(beta-alpha) / (float)(max-min)
@@ -273,7 +297,7 @@ int glsfft_min_max_loc_async(glsfft_context ctx, const float *src, int rows, int
     const size_t n = (size_t)rows * cols;
     cudaError_t e = cudaMemsetAsync(d_keys, 0, 2 * sizeof(unsigned long long), (cudaStream_t)stream);
     if (e != cudaSuccess) return cuda_status(e);
-    minmax_kernel<<<grid_for(n), kThreads, 0, (cudaStream_t)stream>>>(src, n, d_keys);
+    minmax_kernel<<<grid_for(n / 4, 8), kThreads, 0, (cudaStream_t)stream>>>(src, n, d_keys);
     return cuda_status(cudaGetLastError());
 }
 
