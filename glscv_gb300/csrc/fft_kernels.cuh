@@ -190,7 +190,7 @@ __global__ void __launch_bounds__(W *LineFft<N, E>::T)
         // stored, for the normalisation that follows
         static_assert(ST == ST_LOGMAG_MINMAX, "column-pass store variants: complex, log-magnitude");
         __shared__ unsigned long long red[2 * ((W * T + 31) / 32)];
-        unsigned long long kmin = 0, kmax = 0;
+        MinMaxAny run;
         float *fo = reinterpret_cast<float *>(out);
 #pragma unroll
         for (int m = 0; m < E; m++) {
@@ -200,12 +200,10 @@ __global__ void __launch_bounds__(W *LineFft<N, E>::T)
             const float v = spec_log_mag(x[m], a.param);
             if (active) {
                 fo[o] = v;
-                const unsigned long long k0 = min_key(v, o), k1 = max_key(v, o);
-                kmin = k0 > kmin ? k0 : kmin;
-                kmax = k1 > kmax ? k1 : kmax;
+                run.add(v, o);
             }
         }
-        block_minmax_commit(kmin, kmax, red, a.key);
+        block_minmax_commit(run.kmin(), run.kmax(), red, a.key);
     }
 }
 

@@ -76,6 +76,27 @@ __host__ __device__ inline unsigned key_idx(unsigned long long k) {
     return k ? 0xFFFFFFFFu - (unsigned)(k & 0xFFFFFFFFull) : 0u;
 }
 
+// Running min / max of one thread over indices visited in any order: strict
+// compares, equal values resolved to the smaller index; keys are formed once
+// at the end (values at the literal, which the tie rule may have taken, give
+// no key).
+struct MinMaxAny {
+    float vmin = kMinMaxLiteral, vmax = -kMinMaxLiteral;
+    unsigned imin = 0xFFFFFFFFu, imax = 0xFFFFFFFFu;
+    __device__ __forceinline__ void add(float v, unsigned i) {
+        if (v < vmin || (v == vmin && i < imin)) {
+            vmin = v;
+            imin = i;
+        }
+        if (v > vmax || (v == vmax && i < imax)) {
+            vmax = v;
+            imax = i;
+        }
+    }
+    __device__ __forceinline__ unsigned long long kmin() const { return min_key(vmin, imin); }
+    __device__ __forceinline__ unsigned long long kmax() const { return max_key(vmax, imax); }
+};
+
 // Block-wide max of both keys; thread 0 issues the atomics.  `red` holds
 // 2 * (blockDim.x / 32) entries of shared memory.
 __device__ __forceinline__ void block_minmax_commit(unsigned long long kmin,
