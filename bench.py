@@ -56,6 +56,10 @@ def parse():
                         "instead of autotuning it (e.g. 3,1,1,8)")
     p.add_argument("--no-uneven", action="store_true",
                    help="skip the 512-image uneven-size batch section")
+    p.add_argument("--serve-slots", type=int, default=16,
+                   help="request slots (streams in flight) of the serving sweep")
+    p.add_argument("--serving-only", action="store_true",
+                   help="run only the serving sweep and print its JSON")
     p.add_argument("--profile-spectrum", action="store_true",
                    help="run each spectrum operation once on 4096x4096 and exit (for ncu)")
     return p.parse_args()
@@ -221,7 +225,8 @@ SERVE_REFS = [16, 11, 5]          # 32 resident reference spectra
 SERVE_RATES = [1000, 5000, 10000, 20000, 50000]
 
 
-def serving_sweep(g, ctx, torch, seconds: float = 0.5, max_requests: int = 4000) -> dict:
+def serving_sweep(g, ctx, torch, seconds: float = 0.5, max_requests: int = 4000,
+                  slots: int = 16) -> dict:
     """Poisson arrivals (seed 5) of CV_32FC1 frame pairs against 32 resident
     reference spectra; frames are the reference shifted by a seeded integer +
     sub-pixel amount (Fourier shift) plus N(0, 0.01^2); latency = arrival to
@@ -230,7 +235,7 @@ def serving_sweep(g, ctx, torch, seconds: float = 0.5, max_requests: int = 4000)
     from glscv_gb300 import workloads as wl
 
     rng = np.random.default_rng(5)
-    srv = g.Server(ctx, slots=8, hbm_budget=3 << 30)
+    srv = g.Server(ctx, slots=slots, hbm_budget=3 << 30)
     keep, frames_by_size, refs_by_size = [], {}, {}
     for n, count in zip(SERVE_SIZES, SERVE_REFS):
         w = wl.hann_window(n, n)
@@ -255,7 +260,7 @@ def serving_sweep(g, ctx, torch, seconds: float = 0.5, max_requests: int = 4000)
             hb = torch.empty((n, n), dtype=torch.float32, pin_memory=True)
             hb.copy_(torch.from_numpy(b.astype(np.float32)))
             frames_by_size.setdefault(n, []).append((rid0, hb, (sx, sy)))
-    out = {"slots": 8, "hbm_budget_bytes": 3 << 30, "references": sum(SERVE_REFS),
+    out = {"slots": slots, "hbm_budget_bytes": 3 << 30, "references": sum(SERVE_REFS),
            "mix": dict(zip([f"{n}x{n}" for n in SERVE_SIZES], SERVE_MIX)), "rates": [],
            "shift_note": "error vs the synthetic shift is the 5x5 weighted-centroid estimator's "
                          "own bias on sub-pixel shifts (the reference algorithm); deviation vs "
@@ -589,6 +594,11 @@ def run_own(args) -> None:
         torch.cuda.synchronize()
         return max_over_ranks(p0.elapsed_time(p1) / k)
 
+    if args.serving_only:
+        print(json.dumps(serving_sweep(g, ctx, torch, slots=args.serve_slots)), flush=True)
+        ctx.close()
+        return
+
     if args.profile_spectrum:
         # each spectrum operation once (after one warm-up call), for ncu
         spectrum_ops(ctx, torch, s, reps=1, latency=False)
@@ -724,7 +734,8 @@ def run_own(args) -> None:
 
     if rank == 0:
         cb = cpu_baseline(min(args.cpu_sample, B))
-        serving = None if args.no_serving else serving_sweep(g, ctx, torch)
+        serving = None if args.no_serving else serving_sweep(g, ctx, torch,
+                                                             slots=args.serve_slots)
         precision = precision_form(ctx, torch, s)
         uneven = None if args.no_uneven else uneven_batch(g, ctx, torch, s, args.no_autotune)
         spectrum = spectrum_ops(ctx, torch, s)

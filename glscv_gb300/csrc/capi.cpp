@@ -229,8 +229,9 @@ int glsfft::poc_launch(const float2 *tw, const float *src1, const float *src2,
                        const float *window, int rows, int cols, int box, float2 *f1, float2 *f2,
                        float *surface, unsigned long long *key, double *d_result,
                        cudaStream_t s) {
-    cudaError_t e = cudaMemsetAsync(key, 0, sizeof(unsigned long long), s);
-    if (e != cudaSuccess) return cuda_status(e);
+    // three launches: rows of both images; fused POC columns (which also
+    // zero the argmax key and block counter); inverse rows with the argmax
+    // and, in the last block, the centroid
     PassArgs a{};
     a.in0 = src1;
     a.in1 = src2;
@@ -241,7 +242,7 @@ int glsfft::poc_launch(const float2 *tw, const float *src1, const float *src2,
     a.cols = cols;
     a.scale = 1.0f;
     a.tw = tw;
-    e = launch_rows(cols, window ? LD_R1W : LD_R1, ST_C2, a, 2, s);
+    cudaError_t e = launch_rows(cols, window ? LD_R1W : LD_R1, ST_C2, a, 2, s);
     if (e != cudaSuccess) return cuda_status(e);
 
     PassArgs b{};
@@ -251,6 +252,7 @@ int glsfft::poc_launch(const float2 *tw, const float *src1, const float *src2,
     b.rows = rows;
     b.cols = cols;
     b.scale = 1.0f;
+    b.key = key;
     b.tw = tw;
     e = launch_poc_cols(rows, b, s);
     if (e != cudaSuccess) return cuda_status(e);
@@ -264,10 +266,9 @@ int glsfft::poc_launch(const float2 *tw, const float *src1, const float *src2,
     c.flags = PF_SHIFT_ROWS | PF_SHIFT_COLS;
     c.key = key;
     c.tw = tw;
+    c.result = d_result;
+    c.box = box;
     e = launch_rows(cols, LD_C2, ST_RE_ARGMAX, c, 1, s);
-    if (e != cudaSuccess) return cuda_status(e);
-
-    e = launch_poc_finish(surface, rows, cols, box, key, d_result, s);
     return cuda_status(e);
 }
 
@@ -338,7 +339,8 @@ int glsfft_context_create(glsfft_context *out, int device) {
     e = cudaMalloc(&ctx->d_tw, sizeof(float2) * tw.size());
     if (e == cudaSuccess)
         e = cudaMemcpy(ctx->d_tw, tw.data(), sizeof(float2) * tw.size(), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMallocHost(&ctx->h_result, 8 * sizeof(double));
+    if (e == cudaSuccess) e = cudaHostAlloc(&ctx->h_result, 8 * sizeof(double), cudaHostAllocMapped);
+    if (e == cudaSuccess) e = cudaHostGetDevicePointer(&ctx->h_result_dev, ctx->h_result, 0);
     int st = cuda_status(e);
     if (!st) st = tc_tables_create(&ctx->tc);
     if (st) {
@@ -511,16 +513,12 @@ int glsfft_phase_correlate(glsfft_context ctx, const float *src1, const float *s
     if (st) return st;
     DeviceGuard g(ctx->device);
     if (!g.ok()) return GLSFFT_ERROR_CUDA;
-    st = ensure_workspace(ctx, poc_workspace_bytes(rows, cols));
+    // the last block writes the result straight into the context's mapped
+    // pinned buffer: no copy back, one synchronisation
+    st = glsfft_phase_correlate_async(ctx, src1, src2, window, rows, cols, box,
+                                      ctx->h_result_dev, stream);
     if (st) return st;
-    double *d_res = reinterpret_cast<double *>(static_cast<char *>(ctx->ws) +
-                                               poc_result_offset(rows, cols));
-    st = glsfft_phase_correlate_async(ctx, src1, src2, window, rows, cols, box, d_res, stream);
-    if (st) return st;
-    cudaStream_t s = (cudaStream_t)stream;
-    cudaError_t e = cudaMemcpyAsync(ctx->h_result, d_res, 5 * sizeof(double),
-                                    cudaMemcpyDeviceToHost, s);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);
     if (e != cudaSuccess) return cuda_status(e);
     *dx = ctx->h_result[0];
     *dy = ctx->h_result[1];

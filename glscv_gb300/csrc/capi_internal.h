@@ -20,7 +20,8 @@ struct glsfft_context_s {
     void *ws = nullptr;         // workspace (phaseCorrelate scratch)
     size_t ws_bytes = 0;
     size_t budget = 0;          // 0 = unlimited
-    double *h_result = nullptr; // pinned, 8 doubles
+    double *h_result = nullptr; // pinned and mapped, 8 doubles
+    double *h_result_dev = nullptr;  // its device-side address
     glsfft::TcTables tc;        // split-FP16 tensor-core form tables
     const float *surface = nullptr;  // last phaseCorrelate surface
     size_t surface_count = 0;

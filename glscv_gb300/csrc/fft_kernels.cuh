@@ -100,6 +100,45 @@ __device__ __forceinline__ float2 load_elem(const void *img, const float *win, s
     }
 }
 
+// ---------------------------------------------------- centroid finish
+// Decode the argmax key, FP64 weighted centroid over the clamped box in
+// row-major order (glsPhaseCorrelate.cpp:60-137), response divided by
+// rows*cols (:224-225), shift = center - centroid (:228-230).
+// res[0..2] = dx, dy, response; res[3] = peak index as a double, res[4] = peak value.
+// Reads go to L2 (.cg): the surface was written by other blocks of this launch.
+__device__ __forceinline__ void poc_finish(const float *surface, int rows, int cols, int box,
+                                           unsigned long long k, double *res) {
+    int px = 0, py = 0;
+    double peak = -3.402823466e+38;
+    if (k != 0ull) {
+        const unsigned idx = key_index(k);
+        px = (int)(idx % (unsigned)cols);
+        py = (int)(idx / (unsigned)cols);
+        peak = (double)key_value(k);
+    }
+    int minr = py - (box >> 1), maxr = py + (box >> 1);
+    int minc = px - (box >> 1), maxc = px + (box >> 1);
+    if (minr < 0) minr = 0;
+    if (minc < 0) minc = 0;
+    if (maxr > rows - 1) maxr = rows - 1;
+    if (maxc > cols - 1) maxc = cols - 1;
+    double sx = 0.0, sy = 0.0, sum = 0.0;
+    for (int y = minr; y <= maxr; y++)
+        for (int x = minc; x <= maxc; x++) {
+            const double v = (double)__ldcg(surface + (size_t)y * cols + x);
+            sx += (double)x * v;
+            sy += (double)y * v;
+            sum += v;
+        }
+    const double response = sum / ((double)rows * (double)cols);
+    sum += 2.220446049250313e-16;  // DBL_EPSILON, glsPhaseCorrelate.cpp:128
+    res[0] = (double)cols / 2.0 - sx / sum;
+    res[1] = (double)rows / 2.0 - sy / sum;
+    res[2] = response;
+    res[3] = (double)(py * cols + px);
+    res[4] = peak;
+}
+
 // ------------------------------------------------------------- row pass
 // Block: LINES rows x T threads.  blockIdx.y selects the image.  MB bounds
 // the radix (fft_device.cuh).
@@ -147,7 +186,26 @@ __global__ void __launch_bounds__(LINES *LineFft<N, E>::T)
                 best = k > best ? k : best;
             }
         }
-        if constexpr (ST == ST_RE_ARGMAX) block_argmax_commit(best, red, a.key);
+        if constexpr (ST == ST_RE_ARGMAX) {
+            block_argmax_commit(best, red, a.key);
+            if (a.result) {
+                // the last block to finish (every block's surface writes and
+                // key update are released before its count) computes the centroid
+                __shared__ int s_last;
+                if (threadIdx.x == 0) {
+                    __threadfence();
+                    const unsigned long long prev = atomicAdd(a.key + 1, 1ull);
+                    s_last = prev == (unsigned long long)gridDim.x * gridDim.y - 1ull;
+                }
+                __syncthreads();
+                if (s_last && threadIdx.x == 0) {
+                    __threadfence();
+                    poc_finish(reinterpret_cast<const float *>(out), a.rows, N, a.box,
+                               __ldcg(a.key), a.result);
+                    __threadfence_system();  // result may be mapped host memory
+                }
+            }
+        }
     }
 }
 
@@ -231,6 +289,11 @@ __global__ void __launch_bounds__(W *LineFft<N, E>::T)
     const float2 *f1 = reinterpret_cast<const float2 *>(a.in0);
     const float2 *f2 = reinterpret_cast<const float2 *>(a.in1);
     ColSm<W> sm{smem, c};
+    // the argmax key and the block counter of the inverse row pass that follows
+    if (a.key && blockIdx.x == 0 && threadIdx.x == 0) {
+        a.key[0] = 0ull;
+        a.key[1] = 0ull;
+    }
 
     float2 x[E], y[E];
 #pragma unroll
@@ -267,12 +330,5 @@ __global__ void __launch_bounds__(W *LineFft<N, E>::T)
     }
 }
 
-// --------------------------------------------------- centroid finish
-// One thread: decode the argmax key, FP64 weighted centroid over the clamped
-// box in row-major order (glsPhaseCorrelate.cpp:60-137), response divided by
-// rows*cols (:224-225), shift = center - centroid (:228-230).
-// res[0..2] = dx, dy, response; res[3] = peak index as a double, res[4] = peak value.
-__global__ void poc_finish_kernel(const float *surface, int rows, int cols, int box,
-                                  const unsigned long long *key, double *res);
 
 }  // namespace glsfft

@@ -51,6 +51,11 @@ struct PassArgs {
     size_t in_img_bytes;   // batch: byte stride between images (0 = single / in1 mode)
     size_t out_img_bytes;
     float param;       // ST_LOGMAG_MINMAX: the log-magnitude offset
+    // ST_RE_ARGMAX with `result` set: the last block to finish computes the
+    // phaseCorrelate centroid (box edge `box`) into result[0..4]; key[1] is
+    // the block counter (zeroed, with key[0], by the POC column pass)
+    double *result;
+    int box;
 };
 
 // Launchers (fft_rows.cu, fft_cols.cu, poc.cu).  They return cudaSuccess or
@@ -58,8 +63,6 @@ struct PassArgs {
 cudaError_t launch_rows(int n, int ld, int st, const PassArgs &a, int images, cudaStream_t s);
 cudaError_t launch_cols(int n, int ld, int st, const PassArgs &a, int images, cudaStream_t s);
 cudaError_t launch_poc_cols(int n, const PassArgs &a, cudaStream_t s);
-cudaError_t launch_poc_finish(const float *surface, int rows, int cols, int box,
-                              const unsigned long long *key, double *res, cudaStream_t s);
 
 // Twiddle tables: one device buffer of kTwEntries float2 holding the
 // per-pass tables of fft_device.cuh (tw_offset).  Generated in FP64 on the

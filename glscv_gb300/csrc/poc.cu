@@ -1,4 +1,5 @@
-// poc.cu -- fused phaseCorrelate column kernel and the centroid finish.
+// poc.cu -- fused phaseCorrelate column kernel (the centroid finish is fused
+// into the inverse row pass, fft_kernels.cuh).
 #include "fft_config.h"
 #include "fft_kernels.cuh"
 
@@ -36,47 +37,6 @@ cudaError_t launch_poc_cols(int n, const PassArgs &a, cudaStream_t s) {
     case 4096: return poc_t<4096>(a, s);
     default: return cudaErrorInvalidValue;
     }
-}
-
-__global__ void poc_finish_kernel(const float *surface, int rows, int cols, int box,
-                                  const unsigned long long *key, double *res) {
-    if (blockIdx.x != 0 || threadIdx.x != 0) return;
-    const unsigned long long k = *key;
-    int px = 0, py = 0;
-    double peak = -3.402823466e+38;
-    if (k != 0ull) {
-        const unsigned idx = key_index(k);
-        px = (int)(idx % (unsigned)cols);
-        py = (int)(idx / (unsigned)cols);
-        peak = (double)key_value(k);
-    }
-    int minr = py - (box >> 1), maxr = py + (box >> 1);
-    int minc = px - (box >> 1), maxc = px + (box >> 1);
-    if (minr < 0) minr = 0;
-    if (minc < 0) minc = 0;
-    if (maxr > rows - 1) maxr = rows - 1;
-    if (maxc > cols - 1) maxc = cols - 1;
-    double sx = 0.0, sy = 0.0, sum = 0.0;
-    for (int y = minr; y <= maxr; y++)
-        for (int x = minc; x <= maxc; x++) {
-            const double v = (double)surface[(size_t)y * cols + x];
-            sx += (double)x * v;
-            sy += (double)y * v;
-            sum += v;
-        }
-    const double response = sum / ((double)rows * (double)cols);
-    sum += 2.220446049250313e-16;  // DBL_EPSILON, glsPhaseCorrelate.cpp:128
-    res[0] = (double)cols / 2.0 - sx / sum;
-    res[1] = (double)rows / 2.0 - sy / sum;
-    res[2] = response;
-    res[3] = (double)(py * cols + px);
-    res[4] = peak;
-}
-
-cudaError_t launch_poc_finish(const float *surface, int rows, int cols, int box,
-                              const unsigned long long *key, double *res, cudaStream_t s) {
-    poc_finish_kernel<<<1, 32, 0, s>>>(surface, rows, cols, box, key, res);
-    return cudaGetLastError();
 }
 
 }  // namespace glsfft

@@ -4,15 +4,19 @@
 // A server owns one device arena (its whole HBM budget, reserved once), a set
 // of slots (a CUDA stream, an event and a pinned result buffer each), and two
 // native threads:
-//   * the dispatcher admits queued requests in arrival order as soon as a slot
+//   * dispatchers (kDispatchers threads) admit queued requests in arrival
+//     order as soon as a slot
 //     is free and the request's workspace fits in the arena (looking a few
 //     requests past a head that does not fit yet), and launches the request's
 //     whole pipeline on the slot's stream: host->device copy of the frame,
 //     windowed row FFT, phase-only column kernel against the resident
 //     reference spectrum (so 2 FFTs per request instead of 3), inverse row FFT
 //     with the argmax, FP64 centroid, device->host copy of the result;
-//   * the completion poller watches the slots' events, stamps completion
-//     times, returns workspaces to the arena and wakes the dispatcher.
+//   * the completion poller watches the slots' events (queried without the
+//     lock), stamps completion times, returns workspaces to the arena and
+//     wakes the dispatchers.
+// Several dispatchers issue the CUDA calls of different requests at once, so
+// the host's call rate does not cap the request rate.
 // Requests that arrive while others run are admitted as resources free up,
 // so their kernels overlap on the device.  The kernels are deterministic, so
 // a request's result does not depend on what runs beside it.
@@ -60,10 +64,13 @@ struct Request {
 struct Slot {
     cudaStream_t stream = nullptr;
     cudaEvent_t done = nullptr;
-    double *h_result = nullptr;  // pinned, 8 doubles
+    double *h_result = nullptr;      // pinned and mapped, 8 doubles
+    double *h_result_dev = nullptr;  // its device-side address
     long long ticket = -1;
     bool launched = false;  // the event of this ticket's pipeline is recorded
 };
+
+constexpr int kDispatchers = 3;
 
 size_t workspace_bytes(int rows, int cols) {
     const size_t n = (size_t)rows * cols;
@@ -87,7 +94,8 @@ struct glsfft_server_s {
     long long next_ticket = 1;
     int in_flight = 0;
     bool stop = false;
-    std::thread dispatcher, poller;
+    std::vector<std::thread> dispatchers;
+    std::thread poller;
     // counters
     long long admitted = 0, completed = 0, failed = 0;
     long long peak_in_flight = 0, peak_queue = 0;
@@ -105,14 +113,15 @@ int launch_request(glsfft_server srv, const Reference &ref, const Request &rq, S
     float2 *f2 = reinterpret_cast<float2 *>(ws + Arena::round_up(4 * n));
     float *surface = reinterpret_cast<float *>(ws + Arena::round_up(4 * n) + Arena::round_up(8 * n));
     char *tail = ws + Arena::round_up(4 * n) + Arena::round_up(8 * n) + Arena::round_up(4 * n);
-    auto *key = reinterpret_cast<unsigned long long *>(tail);
-    auto *res = reinterpret_cast<double *>(tail + 64);
+    auto *key = reinterpret_cast<unsigned long long *>(tail);  // argmax key, block counter
     const float2 *spec = reinterpret_cast<const float2 *>(srv->d_base + ref.spec_off);
     const float *win = ref.has_window ? reinterpret_cast<const float *>(srv->d_base + ref.win_off) : nullptr;
     cudaStream_t s = slot.stream;
 
+    // five calls: the frame's upload, three launches (the POC column pass
+    // zeroes the argmax key; the last block of the inverse row pass computes
+    // the centroid and writes it into the slot's mapped pinned buffer), the event
     cudaError_t e = cudaMemcpyAsync(frame, rq.frame, 4 * n, cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess) e = cudaMemsetAsync(key, 0, sizeof(unsigned long long), s);
     if (e != cudaSuccess) return cuda_status(e);
     PassArgs a{};
     a.in0 = frame;
@@ -132,6 +141,7 @@ int launch_request(glsfft_server srv, const Reference &ref, const Request &rq, S
     b.cols = cols;
     b.scale = 1.0f;
     b.flags = PF_F1_SPECTRUM;
+    b.key = key;
     b.tw = srv->ctx->d_tw;
     e = launch_poc_cols(rows, b, s);
     if (e != cudaSuccess) return cuda_status(e);
@@ -144,10 +154,9 @@ int launch_request(glsfft_server srv, const Reference &ref, const Request &rq, S
     c.flags = PF_SHIFT_ROWS | PF_SHIFT_COLS;
     c.key = key;
     c.tw = srv->ctx->d_tw;
+    c.result = slot.h_result_dev;
+    c.box = rq.box;
     e = launch_rows(cols, LD_C2, ST_RE_ARGMAX, c, 1, s);
-    if (e == cudaSuccess) e = launch_poc_finish(surface, rows, cols, rq.box, key, res, s);
-    if (e == cudaSuccess)
-        e = cudaMemcpyAsync(slot.h_result, res, 5 * sizeof(double), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaEventRecord(slot.done, s);
     return cuda_status(e);
 }
@@ -212,6 +221,13 @@ void dispatcher_main(glsfft_server srv) {
 
 void poller_main(glsfft_server srv) {
     cudaSetDevice(srv->device);
+    struct Watch {
+        int slot;
+        long long ticket;
+        cudaEvent_t ev;
+    };
+    std::vector<Watch> watch;
+    std::vector<cudaError_t> state;
     std::unique_lock<std::mutex> lock(srv->mu);
     for (;;) {
         if (srv->in_flight == 0) {
@@ -219,15 +235,29 @@ void poller_main(glsfft_server srv) {
             srv->cv_poll.wait(lock);
             continue;
         }
-        bool any = false;
+        // the launched slots, then their events queried without the lock
+        watch.clear();
         for (int i = 0; i < (int)srv->slots.size(); i++) {
-            Slot &slot = srv->slots[i];
-            if (slot.ticket < 0 || !slot.launched) continue;
-            const cudaError_t q = cudaEventQuery(slot.done);
-            if (q == cudaErrorNotReady) continue;
+            const Slot &slot = srv->slots[i];
+            if (slot.ticket >= 0 && slot.launched) watch.push_back({i, slot.ticket, slot.done});
+        }
+        lock.unlock();
+        state.resize(watch.size());
+        bool any_done = false;
+        for (size_t w = 0; w < watch.size(); w++) {
+            state[w] = cudaEventQuery(watch[w].ev);
+            any_done |= state[w] != cudaErrorNotReady;
+        }
+        if (!any_done) std::this_thread::yield();
+        lock.lock();
+        bool any = false;
+        for (size_t w = 0; w < watch.size(); w++) {
+            if (state[w] == cudaErrorNotReady) continue;
+            Slot &slot = srv->slots[watch[w].slot];
+            if (slot.ticket != watch[w].ticket) continue;
             Request &rq = srv->reqs[slot.ticket];
             rq.done_at = Clock::now();
-            if (q == cudaSuccess) {
+            if (state[w] == cudaSuccess) {
                 std::memcpy(rq.result, slot.h_result, sizeof(rq.result));
                 rq.state = REQ_DONE;
                 srv->completed++;
@@ -243,14 +273,8 @@ void poller_main(glsfft_server srv) {
             any = true;
         }
         if (any) {
-            srv->cv_dispatch.notify_one();
+            srv->cv_dispatch.notify_all();
             srv->cv_done.notify_all();
-        } else {
-            // requests are in flight: keep polling (a timed sleep would add
-            // the kernel's timer slack, tens of microseconds, to every latency)
-            lock.unlock();
-            std::this_thread::yield();
-            lock.lock();
         }
     }
 }
@@ -293,7 +317,8 @@ int glsfft_server_create(glsfft_context ctx, int slots, size_t hbm_budget, glsff
     for (auto &s : srv->slots) {
         cudaError_t e = cudaStreamCreateWithFlags(&s.stream, cudaStreamNonBlocking);
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s.done, cudaEventDisableTiming);
-        if (e == cudaSuccess) e = cudaMallocHost(&s.h_result, 8 * sizeof(double));
+        if (e == cudaSuccess) e = cudaHostAlloc(&s.h_result, 8 * sizeof(double), cudaHostAllocMapped);
+        if (e == cudaSuccess) e = cudaHostGetDevicePointer(&s.h_result_dev, s.h_result, 0);
         if (e != cudaSuccess) {
             cudaGetLastError();
             for (auto &t : srv->slots) {
@@ -306,7 +331,7 @@ int glsfft_server_create(glsfft_context ctx, int slots, size_t hbm_budget, glsff
             return GLSFFT_ERROR_CUDA;
         }
     }
-    srv->dispatcher = std::thread(dispatcher_main, srv);
+    for (int i = 0; i < kDispatchers; i++) srv->dispatchers.emplace_back(dispatcher_main, srv);
     srv->poller = std::thread(poller_main, srv);
     *out = srv;
     return GLSFFT_SUCCESS;
@@ -475,7 +500,8 @@ int glsfft_server_destroy(glsfft_server srv) {
     srv->cv_dispatch.notify_all();
     srv->cv_poll.notify_all();
     srv->cv_done.notify_all();
-    if (srv->dispatcher.joinable()) srv->dispatcher.join();
+    for (auto &t : srv->dispatchers)
+        if (t.joinable()) t.join();
     if (srv->poller.joinable()) srv->poller.join();
     DeviceGuard g(srv->device);
     for (auto &s : srv->slots) {
