@@ -501,6 +501,50 @@ def spectrum_ops(ctx, torch, s, reps: int = 5, latency: bool = True) -> dict:
     return out
 
 
+def plain_single(ctx, torch, s) -> dict:
+    """The plain drop-in path one image at a time (gls::fft per call): the
+    256^2 forward + inverse(SCALE) case and single 1024^2 / 4096^2 images
+    (uniform[-1,1) complex, seeds 0, 1, 2), CUDA events (median of 20 calls
+    after 3), with the error against an FP64 DFT."""
+    import numpy as np
+    from glscv_gb300 import workloads as wl
+    out = {}
+    stream = torch.cuda.current_stream()
+    for n, seed in ((256, 0), (1024, 1), (4096, 2)):
+        x = wl.complex_uniform(n, n, seed)
+        d = torch.from_numpy(x).cuda()
+        f = torch.empty_like(d)
+        y = torch.empty_like(d)
+
+        def step():
+            ctx.fft2d(d.data_ptr(), f.data_ptr(), n, n, 0, s)
+            ctx.fft2d(f.data_ptr(), y.data_ptr(), n, n, INV | SCALE, s)
+
+        for _ in range(3):
+            step()
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(20):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            step()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        ts.sort()
+        ms = ts[len(ts) // 2]
+        f64 = np.fft.fft2(x.astype(np.complex128))
+        fh, yh = f.cpu().numpy(), y.cpu().numpy()
+        flops = 2 * 5.0 * n * n * np.log2(n * n)
+        out[f"{n}x{n}"] = {
+            "fwd_inv_ms": round(ms, 4), "gflops": round(flops / (ms * 1e-3) / 1e9, 1),
+            "alg_gbs": round(2 * 32.0 * n * n / (ms * 1e-3) / 1e9, 1),
+            "rel_l2_forward_vs_fp64": float(np.linalg.norm(fh - f64) / np.linalg.norm(f64)),
+            "rel_l2_round_trip": float(np.linalg.norm(yh - x) / np.linalg.norm(x))}
+    return out
+
+
 def g_lib():
     import glscv_gb300
     return glscv_gb300.lib()
@@ -739,6 +783,7 @@ def run_own(args) -> None:
         precision = precision_form(ctx, torch, s)
         uneven = None if args.no_uneven else uneven_batch(g, ctx, torch, s, args.no_autotune)
         spectrum = spectrum_ops(ctx, torch, s)
+        single = plain_single(ctx, torch, s)
         line = {
             "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": round(ms, 4),
@@ -766,6 +811,7 @@ def run_own(args) -> None:
             "precision_form": precision,
             "uneven_batch": uneven,
             "spectrum_ops": spectrum,
+            "plain_single_image": single,
             "clocks": clk,
             "gpu_launches": launches_per_step * args.steps,
         }

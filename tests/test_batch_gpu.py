@@ -112,3 +112,27 @@ def test_batch_argument_errors(ctx, torch_cuda):
         g.Batch(ctx, [d.data_ptr()], [d.data_ptr()], [(8, 8)], (0, 1, 2))
     with pytest.raises(g.GlsError):
         g.Batch(ctx, [d.data_ptr()], [d.data_ptr()], [(8, 8)], (4,))
+
+
+def test_config3_full_512_round_trip_property(ctx, torch_cuda):
+    """The full 512-image uneven batch (sizes drawn with seed 3) forward then
+    INVERSE|SCALE through one plan: every image comes back within FP32
+    round-trip error (a size-independent check at the full configuration)."""
+    torch = torch_cuda
+    shapes = wl.batch_sizes(512, seed=3)
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(3)
+    xs = [torch.empty(sh, dtype=torch.complex64, device="cuda") for sh in shapes]
+    for x in xs:
+        x.view(torch.float32).uniform_(-1, 1, generator=gen)
+    outs = [torch.empty_like(x) for x in xs]
+    s = torch.cuda.current_stream().cuda_stream
+    b = g.Batch(ctx, [x.data_ptr() for x in xs], [o.data_ptr() for o in outs], shapes,
+                (0, INV | SCALE))
+    assert b.info()["persistent_images"] == 512
+    b.execute(s)
+    assert b.status(s) == 0
+    worst = max(float(torch.linalg.vector_norm(o - x) / torch.linalg.vector_norm(x))
+                for x, o in zip(xs, outs))
+    assert worst < 5e-7, worst
+    b.close()
