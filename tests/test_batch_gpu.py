@@ -136,3 +136,34 @@ def test_config3_full_512_round_trip_property(ctx, torch_cuda):
                 for x, o in zip(xs, outs))
     assert worst < 5e-7, worst
     b.close()
+
+
+def test_two_plans_concurrently_on_two_streams(ctx, torch_cuda):
+    """Two persistent launches sized for the whole GPU, queued on two streams at
+    once: blocks of the second start only as the first's retire, and dynamic
+    claiming keeps both correct (no block ever holds an item another waits on
+    without running)."""
+    torch = torch_cuda
+    shapes_a = [(512, 512)] * 24
+    shapes_b = wl.batch_sizes(48, seed=5)
+    plans, ins, outs, refs = [], [], [], []
+    for shapes, seed in ((shapes_a, 1700), (shapes_b, 1800)):
+        b, xs, d_in, d_out, _ = _run_batch(ctx, torch, shapes, (0, INV | SCALE), seed0=seed)
+        plans.append(b)
+        ins.append(d_in)  # the plans keep raw pointers: keep the buffers alive
+        outs.append(d_out)
+        refs.append([d.cpu().numpy().copy() for d in d_out])
+        for d in d_out:
+            d.zero_()
+    torch.cuda.synchronize()
+    s1, s2 = torch.cuda.Stream(), torch.cuda.Stream()
+    for _ in range(3):
+        plans[0].execute(s1.cuda_stream)
+        plans[1].execute(s2.cuda_stream)
+    torch.cuda.synchronize()
+    assert plans[0].status(s1.cuda_stream) == 0 and plans[1].status(s2.cuda_stream) == 0
+    for k in range(2):
+        for i, d in enumerate(outs[k]):
+            assert np.array_equal(d.cpu().numpy().view(np.uint32), refs[k][i].view(np.uint32)), (k, i)
+    for b in plans:
+        b.close()
