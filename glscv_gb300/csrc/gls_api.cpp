@@ -161,10 +161,16 @@ Point2d phaseCorrelate(const GlsMat &src1, const GlsMat &src2, GlsMat &window, d
 
 // ------------------------------------------------------ spectrum operations
 namespace {
-// getDstMat (glsMat.h:173-213): dst keeps its storage when it already has
-// the size and type, else it gets a new image
+// getDstMat (glsMat.h:205-213, the size / type form): dst keeps its storage
+// when it already has the size and type, else it gets a new image
 void dst_for(GlsMat &dst, Size size, int type) {
     if (dst.empty() || dst.size() != size || dst.type() != type) dst = GlsMat(size, type);
+}
+// getDstMat (glsMat.h:173-196, the source form): also a new image when dst
+// shares storage with a source, so other copies of that source keep its data
+void dst_for(GlsMat &dst, const GlsMat &src0, const GlsMat &src1, int type) {
+    if (dst.shares(src0) || dst.shares(src1)) dst = GlsMat();
+    dst_for(dst, src0.size(), type);
 }
 void check_spectrum(const GlsMat &m, const char *where) {
     assert_that(!m.empty() && m.type() == CV_32FC2, where);
@@ -176,7 +182,7 @@ void mulSpectrums(const GlsMat &src0, const GlsMat &src1, GlsMat &dst, bool conj
     check_spectrum(src0, "gls::mulSpectrums: src0 must be CV_32FC2");
     check_spectrum(src1, "gls::mulSpectrums: src1 must be CV_32FC2");
     if (src0.size() != src1.size()) throw Exception(GLSFFT_ERROR_SHAPE, "gls::mulSpectrums");
-    dst_for(dst, src0.size(), CV_32FC2);
+    dst_for(dst, src0, src1, CV_32FC2);
     check(glsfft_mul_spectrums(context(), src0.devptr(), src1.devptr(), dst.devptr(), src0.rows,
                                src0.cols, conj ? 1 : 0, nullptr),
           "gls::mulSpectrums");
@@ -187,7 +193,7 @@ void mulSpectrumsPhaseOnly(const GlsMat &src0, const GlsMat &src1, GlsMat &dst) 
     check_spectrum(src0, "gls::mulSpectrumsPhaseOnly: src0 must be CV_32FC2");
     check_spectrum(src1, "gls::mulSpectrumsPhaseOnly: src1 must be CV_32FC2");
     if (src0.size() != src1.size()) throw Exception(GLSFFT_ERROR_SHAPE, "gls::mulSpectrumsPhaseOnly");
-    dst_for(dst, src0.size(), CV_32FC2);
+    dst_for(dst, src0, src1, CV_32FC2);
     check(glsfft_mul_spectrums_phase_only(context(), src0.devptr(), src1.devptr(), dst.devptr(),
                                           src0.rows, src0.cols, nullptr),
           "gls::mulSpectrumsPhaseOnly");
@@ -230,7 +236,7 @@ void normalize(const GlsMat &src, GlsMat &dst, double alpha, double beta, int no
     // glsNormalize.cpp:52-68
     assert_that(!src.empty() && src.type() == CV_32FC1, "gls::normalize: src must be CV_32FC1");
     assert_that(normType == NORM_MINMAX, "gls::normalize: only NORM_MINMAX is implemented");
-    dst_for(dst, src.size(), CV_32FC1);
+    dst = GlsMat(src.size(), CV_32FC1);  // the reference builds a new _dst and assigns it
     check(glsfft_normalize_minmax(context(), static_cast<const float *>(src.devptr()),
                                   static_cast<float *>(dst.devptr()), src.rows, src.cols, alpha,
                                   beta, nullptr),

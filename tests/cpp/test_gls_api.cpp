@@ -220,6 +220,14 @@ static void test_spectrum_ops() {
     Mat hn = nrm;
     EXPECT(hn.ptr<float>()[2 * C + 30] == 0.f && std::fabs(hn.ptr<float>()[5 * C + 7] - 1.f) < 1e-6f,
            "normalize NORM_MINMAX maps min to 0 and max to 1");
+    // getDstMat: an output that aliases an input gets new storage, so other
+    // copies of the input keep its data (glsMat.h:173-196)
+    GlsMat a2(a), keep = a2;
+    gls::mulSpectrums(a2, gb, a2, false);
+    Mat hk = keep, ha2 = a2;
+    EXPECT(!a2.shares(keep), "mulSpectrums into its own input gets new storage");
+    EXPECT(hk.ptr<float>()[0] == a.ptr<float>()[0] && ha2.ptr<float>()[0] == hp.ptr<float>()[0],
+           "the old copy keeps the input, the output has the product");
     bool thrown = false;
     try {
         gls::normalize(gimg, nrm, 1, 0, gls::NORM_L2);
