@@ -113,6 +113,26 @@ void glsCvTerminate() {
 
 glsfft_context glsCvContext() { return context(); }
 
+// ------------------------------------------------------------ outputs
+// The output image of an operation, chosen before dst is assigned (dst may
+// be the same object as a source, which must stay valid while it is read);
+// the operation computes into it and assigns dst = out at the end, as the
+// reference's `_dst = getDstMat(...); ...; dst = _dst;` does.
+namespace {
+// getDstMat (glsMat.h:205-213, the size / type form): dst's storage when it
+// already has the size and type, else a new image
+GlsMat out_for(const GlsMat &dst, Size size, int type) {
+    if (dst.empty() || dst.size() != size || dst.type() != type) return GlsMat(size, type);
+    return dst;
+}
+// getDstMat (glsMat.h:173-196, the source form): also a new image when dst
+// shares storage with a source, so other copies of that source keep its data
+GlsMat out_for(const GlsMat &dst, const GlsMat &src0, const GlsMat &src1, int type) {
+    if (dst.shares(src0) || dst.shares(src1)) return GlsMat(src0.size(), type);
+    return out_for(dst, src0.size(), type);
+}
+}  // namespace
+
 // ------------------------------------------------------------------ fft
 void fft(const GlsMat &src, GlsMat &dst, int flag) {
     // glsFft.cpp:676-681
@@ -120,15 +140,17 @@ void fft(const GlsMat &src, GlsMat &dst, int flag) {
     assert_that(src.channels() == 2 || src.channels() == 1, "gls::fft: channels must be 1 or 2");
     assert_that(src.depth() == CV_32F, "gls::fft: depth must be CV_32F");
     glsfft_context ctx = context();
-    if (dst.empty() || dst.size() != src.size() || dst.type() != CV_32FC2)
-        dst = GlsMat(src.size(), CV_32FC2);
+    // the output is chosen before dst is touched: dst may be the very object
+    // src refers to (fft(C, C)), and src must stay valid while it is read
+    GlsMat out = out_for(dst, src.size(), CV_32FC2);
     int st;
     if (src.channels() == 2)
-        st = glsfft_fft2d_c2c(ctx, src.devptr(), dst.devptr(), src.rows, src.cols, flag, nullptr);
+        st = glsfft_fft2d_c2c(ctx, src.devptr(), out.devptr(), src.rows, src.cols, flag, nullptr);
     else
-        st = glsfft_fft2d_r2c_promote(ctx, static_cast<const float *>(src.devptr()), dst.devptr(),
+        st = glsfft_fft2d_r2c_promote(ctx, static_cast<const float *>(src.devptr()), out.devptr(),
                                       src.rows, src.cols, flag, nullptr);
     check(st, "gls::fft");
+    dst = out;
 }
 
 void ifft(const GlsMat &src, GlsMat &dst, int flag) { fft(src, dst, flag | GLS_FFT_INVERSE); }
@@ -161,17 +183,6 @@ Point2d phaseCorrelate(const GlsMat &src1, const GlsMat &src2, GlsMat &window, d
 
 // ------------------------------------------------------ spectrum operations
 namespace {
-// getDstMat (glsMat.h:205-213, the size / type form): dst keeps its storage
-// when it already has the size and type, else it gets a new image
-void dst_for(GlsMat &dst, Size size, int type) {
-    if (dst.empty() || dst.size() != size || dst.type() != type) dst = GlsMat(size, type);
-}
-// getDstMat (glsMat.h:173-196, the source form): also a new image when dst
-// shares storage with a source, so other copies of that source keep its data
-void dst_for(GlsMat &dst, const GlsMat &src0, const GlsMat &src1, int type) {
-    if (dst.shares(src0) || dst.shares(src1)) dst = GlsMat();
-    dst_for(dst, src0.size(), type);
-}
 void check_spectrum(const GlsMat &m, const char *where) {
     assert_that(!m.empty() && m.type() == CV_32FC2, where);
 }
@@ -182,10 +193,11 @@ void mulSpectrums(const GlsMat &src0, const GlsMat &src1, GlsMat &dst, bool conj
     check_spectrum(src0, "gls::mulSpectrums: src0 must be CV_32FC2");
     check_spectrum(src1, "gls::mulSpectrums: src1 must be CV_32FC2");
     if (src0.size() != src1.size()) throw Exception(GLSFFT_ERROR_SHAPE, "gls::mulSpectrums");
-    dst_for(dst, src0, src1, CV_32FC2);
-    check(glsfft_mul_spectrums(context(), src0.devptr(), src1.devptr(), dst.devptr(), src0.rows,
+    GlsMat out = out_for(dst, src0, src1, CV_32FC2);
+    check(glsfft_mul_spectrums(context(), src0.devptr(), src1.devptr(), out.devptr(), src0.rows,
                                src0.cols, conj ? 1 : 0, nullptr),
           "gls::mulSpectrums");
+    dst = out;
 }
 
 void mulSpectrumsPhaseOnly(const GlsMat &src0, const GlsMat &src1, GlsMat &dst) {
@@ -193,30 +205,31 @@ void mulSpectrumsPhaseOnly(const GlsMat &src0, const GlsMat &src1, GlsMat &dst) 
     check_spectrum(src0, "gls::mulSpectrumsPhaseOnly: src0 must be CV_32FC2");
     check_spectrum(src1, "gls::mulSpectrumsPhaseOnly: src1 must be CV_32FC2");
     if (src0.size() != src1.size()) throw Exception(GLSFFT_ERROR_SHAPE, "gls::mulSpectrumsPhaseOnly");
-    dst_for(dst, src0, src1, CV_32FC2);
-    check(glsfft_mul_spectrums_phase_only(context(), src0.devptr(), src1.devptr(), dst.devptr(),
+    GlsMat out = out_for(dst, src0, src1, CV_32FC2);
+    check(glsfft_mul_spectrums_phase_only(context(), src0.devptr(), src1.devptr(), out.devptr(),
                                           src0.rows, src0.cols, nullptr),
           "gls::mulSpectrumsPhaseOnly");
+    dst = out;
 }
 
 void magSpectrums(const GlsMat &src, GlsMat &dst) {
     // glsBasicOperation.cpp:337-343
     check_spectrum(src, "gls::magSpectrums: src must be CV_32FC2");
-    if (dst.shares(src)) dst = GlsMat();
-    dst_for(dst, src.size(), CV_32FC1);
-    check(glsfft_mag_spectrums(context(), src.devptr(), static_cast<float *>(dst.devptr()),
+    GlsMat out = out_for(dst, src.size(), CV_32FC1);  // a CV_32FC1 never shares a CV_32FC2
+    check(glsfft_mag_spectrums(context(), src.devptr(), static_cast<float *>(out.devptr()),
                                src.rows, src.cols, nullptr),
           "gls::magSpectrums");
+    dst = out;
 }
 
 void logMagSpectrums(const GlsMat &src, GlsMat &dst, float offset) {
     // glsBasicOperation.cpp:345-351
     check_spectrum(src, "gls::logMagSpectrums: src must be CV_32FC2");
-    if (dst.shares(src)) dst = GlsMat();
-    dst_for(dst, src.size(), CV_32FC1);
-    check(glsfft_log_mag_spectrums(context(), src.devptr(), static_cast<float *>(dst.devptr()),
+    GlsMat out = out_for(dst, src.size(), CV_32FC1);
+    check(glsfft_log_mag_spectrums(context(), src.devptr(), static_cast<float *>(out.devptr()),
                                    src.rows, src.cols, offset, nullptr),
           "gls::logMagSpectrums");
+    dst = out;
 }
 
 void minMaxLoc(const GlsMat &src, double *minVal, double *maxVal, Point *minLoc, Point *maxLoc,
@@ -236,11 +249,12 @@ void normalize(const GlsMat &src, GlsMat &dst, double alpha, double beta, int no
     // glsNormalize.cpp:52-68
     assert_that(!src.empty() && src.type() == CV_32FC1, "gls::normalize: src must be CV_32FC1");
     assert_that(normType == NORM_MINMAX, "gls::normalize: only NORM_MINMAX is implemented");
-    dst = GlsMat(src.size(), CV_32FC1);  // the reference builds a new _dst and assigns it
+    GlsMat out(src.size(), CV_32FC1);  // the reference builds a new _dst and assigns it
     check(glsfft_normalize_minmax(context(), static_cast<const float *>(src.devptr()),
-                                  static_cast<float *>(dst.devptr()), src.rows, src.cols, alpha,
+                                  static_cast<float *>(out.devptr()), src.rows, src.cols, alpha,
                                   beta, nullptr),
           "gls::normalize");
+    dst = out;
 }
 
 }  // namespace gls

@@ -228,6 +228,16 @@ static void test_spectrum_ops() {
     EXPECT(!a2.shares(keep), "mulSpectrums into its own input gets new storage");
     EXPECT(hk.ptr<float>()[0] == a.ptr<float>()[0] && ha2.ptr<float>()[0] == hp.ptr<float>()[0],
            "the old copy keeps the input, the output has the product");
+    // a CV_32FC1 image transformed into itself (dst is the same object as src)
+    Mat r1(16, 16, gls::CV_32FC1);
+    for (size_t i = 0; i < r1.total(); i++) r1.ptr<float>()[i] = (float)std::cos(0.11 * i);
+    GlsMat self(r1), ref_out;
+    gls::fft(self, ref_out);
+    gls::fft(self, self);
+    Mat hs = self, hr = ref_out;
+    bool eq = self.type() == gls::CV_32FC2;
+    for (size_t i = 0; i < 2 * hs.total(); i++) eq &= hs.ptr<float>()[i] == hr.ptr<float>()[i];
+    EXPECT(eq, "fft(C, C) of a CV_32FC1 image");
     bool thrown = false;
     try {
         gls::normalize(gimg, nrm, 1, 0, gls::NORM_L2);
