@@ -53,7 +53,7 @@ struct PassShape {
 
 __host__ __device__ constexpr int ilog2s(int n) { return n <= 1 ? 0 : 1 + ilog2s(n >> 1); }
 
-__host__ __device__ constexpr PassShape shape_variant(int n, PassShape d, int id) {
+__host__ __device__ constexpr PassShape shape_variant(PassShape d, int id) {
     return id == 1 ? PassShape{d.E / 2, cmin(4, ilog2s(d.E / 2)), d.G}
          : id == 2 ? PassShape{d.E * 2, 4, d.G}
          : id == 3 ? PassShape{d.E, 4, d.G / 2}
@@ -61,10 +61,10 @@ __host__ __device__ constexpr PassShape shape_variant(int n, PassShape d, int id
                    : d;
 }
 __host__ __device__ constexpr PassShape row_shape(int n, int id) {
-    return shape_variant(n, PassShape{rows_E(n), 4, rows_LINES(n)}, id);
+    return shape_variant(PassShape{rows_E(n), 4, rows_LINES(n)}, id);
 }
 __host__ __device__ constexpr PassShape col_shape(int n, int id) {
-    return shape_variant(n, PassShape{cols_E(n), 4, cols_W(n)}, id);
+    return shape_variant(PassShape{cols_E(n), 4, cols_W(n)}, id);
 }
 // threads per block of a shape
 __host__ __device__ constexpr int shape_threads(int n, PassShape s) { return s.G * (n / s.E); }
