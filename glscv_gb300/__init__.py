@@ -40,6 +40,7 @@ _SIGNATURES = {
     "glsfft_context_destroy": (_ip, [_vp]),
     "glsfft_context_set_budget": (_ip, [_vp, _sz]),
     "glsfft_context_workspace": (_ip, [_vp, ctypes.POINTER(_sz)]),
+    "glsfft_device_status": (_ip, [_vp, _ip]),
     "glsfft_fft2d_c2c": (_ip, [_vp, _vp, _vp, _ip, _ip, _ip, _vp]),
     "glsfft_fft2d_r2c_promote": (_ip, [_vp, _vp, _vp, _ip, _ip, _ip, _vp]),
     "glsfft_fft_rows": (_ip, [_vp, _vp, _vp, _ip, _ip, _ip, _ip, _vp]),
@@ -201,6 +202,11 @@ class Context:
         b = _sz()
         check(lib().glsfft_context_workspace(self.handle, ctypes.byref(b)), "workspace")
         return b.value
+
+    def device_status(self, clear: bool = False) -> int:
+        """Sticky status of the context's device-side bounded waits (0 = none
+        expired); synchronises with the device."""
+        return int(lib().glsfft_device_status(self.handle, int(clear)))
 
     def set_budget(self, nbytes: int) -> None:
         check(lib().glsfft_context_set_budget(self.handle, nbytes), "set_budget")

@@ -182,20 +182,25 @@ PFN_cuTensorMapEncodeTiled_v12000 tmap_encoder() {
 
 }  // namespace
 
-int glsfft::make_column_tmap(void *tmap128, const void *img, int rows, int cols) {
+int glsfft::make_tmap_2d(void *tmap128, const void *base, long long width, long long height,
+                         int box_w, int box_h) {
     auto enc = tmap_encoder();
     if (!enc) return GLSFFT_ERROR_CUDA;
-    const int w = kBatchTileElems / rows;     // columns per tile
-    const int br = rows < 256 ? rows : 256;   // box height (TMA box dims <= 256)
-    cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
-    cuuint64_t strides[1] = {(cuuint64_t)cols * sizeof(float2)};
-    cuuint32_t box[2] = {(cuuint32_t)w, (cuuint32_t)br};
+    cuuint64_t dims[2] = {(cuuint64_t)width, (cuuint64_t)height};
+    cuuint64_t strides[1] = {(cuuint64_t)width * sizeof(float2)};
+    cuuint32_t box[2] = {(cuuint32_t)box_w, (cuuint32_t)box_h};
     cuuint32_t estr[2] = {1, 1};
     CUresult r = enc(reinterpret_cast<CUtensorMap *>(tmap128), CU_TENSOR_MAP_DATA_TYPE_UINT64, 2,
-                     const_cast<void *>(img), dims, strides, box, estr,
+                     const_cast<void *>(base), dims, strides, box, estr,
                      CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
                      CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     return r == CUDA_SUCCESS ? GLSFFT_SUCCESS : GLSFFT_ERROR_CUDA;
+}
+
+int glsfft::make_column_tmap(void *tmap128, const void *img, int rows, int cols) {
+    const int w = kBatchTileElems / rows;     // columns per tile
+    const int br = rows < 256 ? rows : 256;   // box height (TMA box dims <= 256)
+    return make_tmap_2d(tmap128, img, cols, rows, w, br);
 }
 
 extern "C" {

@@ -200,6 +200,7 @@ int glsfft::fft2d_launch(glsfft_context ctx, const void *src, void *dst, int row
         a.flags = (inv ? PF_CONJ_IN : 0u) | (inv && !do_cols ? PF_CONJ_OUT : 0u) |
                   (shift ? PF_SHIFT_COLS : 0u);
         a.tw = ctx->d_tw;
+        a.err = ctx->d_status;
         a.in_img_bytes = px * (real_in ? sizeof(float) : sizeof(float2));
         a.out_img_bytes = px * sizeof(float2);
         cudaError_t e = real_in ? launch_rows(cols, LD_R1, ST_C2, a, count, s)
@@ -216,6 +217,7 @@ int glsfft::fft2d_launch(glsfft_context ctx, const void *src, void *dst, int row
         a.flags = (inv && !do_rows ? PF_CONJ_IN : 0u) | (inv ? PF_CONJ_OUT : 0u) |
                   (shift ? PF_SHIFT_ROWS : 0u);
         a.tw = ctx->d_tw;
+        a.err = ctx->d_status;
         a.in_img_bytes = a.out_img_bytes = px * sizeof(float2);
         cudaError_t e = launch_cols_sched(rows, sc.col, a, count, s);
         if (e != cudaSuccess) return cuda_status(e);
@@ -341,12 +343,15 @@ int glsfft_context_create(glsfft_context *out, int device) {
         e = cudaMemcpy(ctx->d_tw, tw.data(), sizeof(float2) * tw.size(), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaHostAlloc(&ctx->h_result, 8 * sizeof(double), cudaHostAllocMapped);
     if (e == cudaSuccess) e = cudaHostGetDevicePointer(&ctx->h_result_dev, ctx->h_result, 0);
+    if (e == cudaSuccess) e = cudaMalloc(&ctx->d_status, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(ctx->d_status, 0, sizeof(int));
     int st = cuda_status(e);
     if (!st) st = tc_tables_create(&ctx->tc);
     if (st) {
         cudaGetLastError();
         if (ctx->d_tw) cudaFree(ctx->d_tw);
         if (ctx->h_result) cudaFreeHost(ctx->h_result);
+        if (ctx->d_status) cudaFree(ctx->d_status);
         delete ctx;
         return st;
     }
@@ -361,9 +366,21 @@ int glsfft_context_destroy(glsfft_context ctx) {
     if (ctx->ws) cudaFree(ctx->ws);
     if (ctx->d_tw) cudaFree(ctx->d_tw);
     if (ctx->h_result) cudaFreeHost(ctx->h_result);
+    if (ctx->d_status) cudaFree(ctx->d_status);
     tc_tables_destroy(&ctx->tc);
     delete ctx;
     return GLSFFT_SUCCESS;
+}
+
+int glsfft_device_status(glsfft_context ctx, int clear) {
+    if (!ctx) return GLSFFT_ERROR_INVALID_VALUE;
+    DeviceGuard g(ctx->device);
+    if (!g.ok()) return GLSFFT_ERROR_CUDA;
+    int v = 0;
+    cudaError_t e = cudaMemcpy(&v, ctx->d_status, sizeof(int), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && clear && v) e = cudaMemset(ctx->d_status, 0, sizeof(int));
+    if (e != cudaSuccess) return cuda_status(e);
+    return v;
 }
 
 int glsfft_fft2d_tc(glsfft_context ctx, const void *src, void *dst, int count, int rows,
@@ -451,6 +468,7 @@ static int one_pass(glsfft_context ctx, const void *src, void *dst, int count, i
     a.flags = (inv ? PF_CONJ_IN | PF_CONJ_OUT : 0u) |
               ((flags & GLSFFT_SHIFT) ? (along_rows ? PF_SHIFT_COLS : PF_SHIFT_ROWS) : 0u);
     a.tw = ctx->d_tw;
+    a.err = ctx->d_status;
     a.in_img_bytes = a.out_img_bytes = (size_t)rows * cols * sizeof(float2);
     FftSchedule sc{};
     const auto it = ctx->sched.find(sched_key(rows, cols));

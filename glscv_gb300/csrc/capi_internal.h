@@ -29,6 +29,7 @@ struct glsfft_context_s {
     // launches use; sizes not listed run schedule 0
     std::map<long long, glsfft::FftSchedule> sched;
     HostPipe *host_pipe = nullptr;  // glsfft_fft2d_host's pipeline, built on first use
+    int *d_status = nullptr;  // device status word of bounded waits (glsfft_device_status)
 };
 
 namespace glsfft {

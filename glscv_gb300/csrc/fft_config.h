@@ -40,11 +40,17 @@ __host__ __device__ constexpr int padded_count(int count) { return count + (coun
 //      thread per pass), half the threads per line
 //   3: half the lines (rows) or columns (cols) per block
 //   4: twice the lines or columns per block
-// A schedule exists for N >= kSchedMinLen when its block has 32..1024
+//   5: 1 and 3 together (half the elements per thread, half the lines or
+//      columns per block: smaller blocks, more of them resident per SM)
+//   6: streamed (fft_stream.cu): one persistent block per SM that copies
+//      the next 128 KB tile in with the TMA while it transforms the current
+//      one; 2048- and 4096-point lines only, bit-identical to schedule 0
+// Schedules 1..5 exist for N >= kSchedMinLen when the block has 32..1024
 // threads, fits 227 KB of shared memory and its E divides N; every
 // schedule computes the same transform (the rounding differs with the radix
 // order, within the FP32 error bound).
-constexpr int kPassSchedules = 5;
+constexpr int kPassSchedules = 7;
+constexpr int kSchedStreamed = 6;
 constexpr int kSchedMinLen = 64;
 
 struct PassShape {
@@ -58,6 +64,7 @@ __host__ __device__ constexpr PassShape shape_variant(PassShape d, int id) {
          : id == 2 ? PassShape{d.E * 2, 4, d.G}
          : id == 3 ? PassShape{d.E, 4, d.G / 2}
          : id == 4 ? PassShape{d.E, 4, d.G * 2}
+         : id == 5 ? PassShape{d.E / 2, cmin(4, ilog2s(d.E / 2)), d.G / 2}
                    : d;
 }
 __host__ __device__ constexpr PassShape row_shape(int n, int id) {
@@ -85,8 +92,8 @@ __host__ __device__ constexpr bool same_shape(PassShape a, PassShape b) {
 // whether schedule `id` of a row (cols=false) or column pass of length n
 // exists and differs from schedule 0
 __host__ __device__ constexpr bool sched_available(int n, int id, bool cols) {
-    return id == 0 ||
-           (id > 0 && id < kPassSchedules && n >= kSchedMinLen && n <= 4096 &&
+    return id == 0 || (id == kSchedStreamed && (n == 2048 || n == 4096)) ||
+           (id > 0 && id < kSchedStreamed && n >= kSchedMinLen && n <= 4096 &&
             shape_ok(n, cols ? col_shape(n, id) : row_shape(n, id), cols) &&
             !same_shape(cols ? col_shape(n, id) : row_shape(n, id),
                         cols ? col_shape(n, 0) : row_shape(n, 0)));

@@ -286,7 +286,10 @@ struct Strided {
     static constexpr int STEP = by_block ? LIN + LIN / 16 : LIN;
 };
 
-// Sm: shared-memory accessor (at(pos) -> float2*, KW) for this thread's line.
+// Sm: shared-memory accessor for this thread's line: at(pos) -> float2*
+// (one exchange of complex values, KW as above), or, with Sm::kSplit,
+// at(pos) -> float* (the exchange runs twice through a buffer half the size,
+// real parts then imaginary parts).
 // tw: the per-pass twiddle tables above.
 template <int N, int E, class Sync = SyncBlock, int MB = 4>
 struct LineFft {
@@ -339,7 +342,7 @@ struct LineFft {
                     }
                 }
                 Dft<R>::run(v);
-                if constexpr (last) {
+                if constexpr (last || Sm::kSplit) {
 #pragma unroll
                     for (int r = 0; r < R; r++) x[s + r * S] = v[r];
                 } else {
@@ -355,7 +358,11 @@ struct LineFft {
                     }
                 }
             }
-            if constexpr (!last) {
+            if constexpr (!last && Sm::kSplit) {
+                exchange_half<p, 0>(x, t, sm);
+                exchange_half<p, 1>(x, t, sm);
+                pass<p + 1>(x, t, sm, tw);
+            } else if constexpr (!last) {
                 sync();
                 using RS = Strided<Sm, T, E>;
                 if constexpr (RS::affine) {
@@ -372,6 +379,35 @@ struct LineFft {
                 pass<p + 1>(x, t, sm, tw);
             }
         }
+    }
+
+    // One component (H = 0: real, 1: imaginary) of the exchange after pass
+    // p, through a float buffer: the butterfly outputs, still in x in their
+    // pass order, go to their Stockham positions; the reads bring back
+    // positions t + m*T.  The other component's registers are untouched, so
+    // the second half still sees the pre-exchange order.
+    template <int p, int H, class Sm>
+    __device__ __forceinline__ static void exchange_half(float2 (&x)[E], int t, Sm sm) {
+        const Sync sync{};
+        constexpr int R = pass_radix(N, p, MB);
+        constexpr int Ns = pass_span(N, p, MB);
+        constexpr int S = E / R;
+#pragma unroll
+        for (int s = 0; s < S; s++) {
+            const int j = t + s * T;
+            const int d = (j / Ns) * Ns * R + (j & (Ns - 1));
+#pragma unroll
+            for (int r = 0; r < R; r++) *sm.at(d + r * Ns) = H ? x[s + r * S].y : x[s + r * S].x;
+        }
+        sync();
+#pragma unroll
+        for (int m = 0; m < E; m++) {
+            const float v = *sm.at(t + m * T);
+            if constexpr (H == 0) x[m].x = v;
+            else x[m].y = v;
+        }
+        // the second half, or the next exchange, overwrites the buffer
+        if constexpr (H == 0 || p + 2 < P) sync();
     }
 };
 

@@ -24,6 +24,7 @@ namespace glsfft {
 // values keeps the stride-R butterfly writes of the first exchange on
 // distinct banks.
 struct RowSm {
+    static constexpr bool kSplit = false;
     static constexpr int KW = 1;
     float2 *base;
     __device__ __forceinline__ float2 *at(int pos) const { return base + pos + (pos >> 4); }
@@ -32,6 +33,7 @@ struct RowSm {
 // per-16 padding over the linearised index.
 template <int W>
 struct ColSm {
+    static constexpr bool kSplit = false;
     static constexpr int KW = W;
     float2 *base;
     int c;
@@ -40,6 +42,31 @@ struct ColSm {
         return base + i + (i >> 4);
     }
 };
+
+// Split-exchange accessors (real and imaginary parts exchanged in turn
+// through a float buffer of half the size).  Rows pad one float per 32,
+// columns two per 32: with 16 values per thread and radix-16 passes on
+// 2048- and 4096-point lines these keep the stores and loads of a warp on
+// distinct banks, except the second row exchange's stores (two-way).
+struct RowSmF {
+    static constexpr bool kSplit = true;
+    static constexpr int KW = 1;
+    float *base;
+    __device__ __forceinline__ float *at(int pos) const { return base + pos + (pos >> 5); }
+};
+template <int W>
+struct ColSmF {
+    static constexpr bool kSplit = true;
+    static constexpr int KW = W;
+    float *base;
+    int c;
+    __device__ __forceinline__ float *at(int pos) const {
+        const int i = pos * W + c;
+        return base + i + 2 * (i >> 5);
+    }
+};
+__host__ __device__ constexpr int row_split_floats(int n) { return n + (n >> 5); }
+__host__ __device__ constexpr int col_split_floats(int count) { return count + 2 * (count >> 5); }
 
 // Whole-line conjugation and scaling behind uniform branches, so the common
 // flag-free case spends no instructions per element.

@@ -47,6 +47,12 @@ cudaError_t launch_cols_sched(int n, int id, const PassArgs &a, int images, cuda
     case 2: return cols_id<2>(n, a, images, s);
     case 3: return cols_id<3>(n, a, images, s);
     case 4: return cols_id<4>(n, a, images, s);
+    case 5: return cols_id<5>(n, a, images, s);
+    case kSchedStreamed: {
+        // arguments the streamed pass does not take run schedule 0
+        if (!stream_pass_applies(n, true, a, images)) return launch_cols(n, LD_C2, ST_C2, a, images, s);
+        return launch_stream_pass(n, true, a, images, s);
+    }
     default: return cudaErrorInvalidValue;
     }
 }

@@ -56,6 +56,9 @@ struct PassArgs {
     // the block counter (zeroed, with key[0], by the POC column pass)
     double *result;
     int box;
+    // device status word for bounded waits (the streamed passes record
+    // GLSFFT_ERROR_TIMEOUT there), or null
+    int *err;
 };
 
 // Launchers (fft_rows.cu, fft_cols.cu, poc.cu).  They return cudaSuccess or
@@ -63,6 +66,19 @@ struct PassArgs {
 cudaError_t launch_rows(int n, int ld, int st, const PassArgs &a, int images, cudaStream_t s);
 cudaError_t launch_cols(int n, int ld, int st, const PassArgs &a, int images, cudaStream_t s);
 cudaError_t launch_poc_cols(int n, const PassArgs &a, cudaStream_t s);
+
+// Streamed passes for 2048- and 4096-point lines (fft_stream.cu): whether
+// the pass applies to these arguments (contiguous complex images, 16-byte
+// aligned, the line count a multiple of the tile's), and the launch, which
+// gives cudaErrorNotSupported when it does not apply.
+bool stream_pass_applies(int n, bool cols, const PassArgs &a, int images);
+cudaError_t launch_stream_pass(int n, bool cols, const PassArgs &a, int images, cudaStream_t s);
+
+// A 2-D tensor map over a row-major array of 8-byte elements (width x
+// height, rows `width` elements apart) with a box_w x box_h box, for TMA
+// copies (batch.cpp).  GLSFFT_SUCCESS or an error status.
+int make_tmap_2d(void *tmap128, const void *base, long long width, long long height, int box_w,
+                 int box_h);
 
 // Twiddle tables: one device buffer of kTwEntries float2 holding the
 // per-pass tables of fft_device.cuh (tw_offset).  Generated in FP64 on the

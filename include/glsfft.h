@@ -79,6 +79,13 @@ GLSFFT_API int glsfft_context_set_budget(glsfft_context ctx, size_t bytes);
 /* Bytes of device workspace the context currently holds. */
 GLSFFT_API int glsfft_context_workspace(glsfft_context ctx, size_t *bytes);
 
+/* Sticky status of the context's device-side bounded waits outside batch
+ * plans and servers (the streamed passes' tile waits): GLSFFT_SUCCESS, or
+ * GLSFFT_ERROR_TIMEOUT once a wait expired (that pass's output is then
+ * incomplete).  Synchronises with the device; `clear` resets the word.  No
+ * reference counterpart. */
+GLSFFT_API int glsfft_device_status(glsfft_context ctx, int clear);
+
 /*
  * 2-D complex FFT of a CV_32FC2 rows x cols device image:
  * gls::fft(src, dst, flag), glsCV/glsFft.h:55 / glsFft.cpp:675-708.
@@ -134,14 +141,19 @@ GLSFFT_API int glsfft_fft2d_tc(glsfft_context ctx, const void *src, void *dst, i
 /*
  * Pass schedules of the plain path (no reference counterpart: glsCV runs
  * one fixed radix-4 schedule, glsFft.cpp:494-671).  The complex row pass and
- * column pass each have schedules 0..4 per line length: 0 the default;
+ * column pass each have schedules 0..6 per line length: 0 the default;
  * 1 half the elements per thread with the radix bound lowered to match;
  * 2 twice the elements per thread; 3 / 4 half / twice the lines or columns
- * per block.  All compute the same transform (rounding differs with the
- * radix order, within the FP32 error bound).  Schedules other than 0 exist
- * for lengths 64..4096 where the block fits the SM.
+ * per block; 5 = 1 and 3 together; 6 streamed: one persistent block per SM
+ * that copies the next 128 KB tile in with the TMA while it transforms the
+ * current one (lengths 2048 and 4096; bit-identical to schedule 0; calls
+ * whose buffers are not 16-byte aligned run schedule 0).  All compute the
+ * same transform (rounding differs with the radix order, within the FP32
+ * error bound).  Schedules 1..5 exist for lengths 64..4096 where the block
+ * fits the SM.
  */
-#define GLSFFT_PASS_SCHEDULES 5
+#define GLSFFT_PASS_SCHEDULES 7
+#define GLSFFT_SCHEDULE_STREAMED 6
 /* 1 when `schedule` exists for a row pass (along_cols = 0) or column pass
  * (along_cols = 1) of line length `length`, else 0. */
 GLSFFT_API int glsfft_schedule_available(int length, int schedule, int along_cols);

@@ -41,8 +41,8 @@ def test_every_schedule_matches_oracle(tctx, torch_cuda, oracle, shape):
     small = max(rows, cols) <= 1024
     ref = oracle.fft2d(x, 0, 1) if small else None
     eps = oracle.fft_eps(max(rows, cols), 0) * 2
-    pairs = [(r, 0) for r in range(5) if g.schedule_available(cols, r, False)]
-    pairs += [(0, c) for c in range(1, 5) if g.schedule_available(rows, c, True)]
+    pairs = [(r, 0) for r in range(7) if g.schedule_available(cols, r, False)]
+    pairs += [(0, c) for c in range(1, 7) if g.schedule_available(rows, c, True)]
     assert len(pairs) >= 5
     for r, c in pairs:
         tctx.set_fft_schedule(rows, cols, r, c)
@@ -85,7 +85,7 @@ def test_unavailable_schedules_are_refused(tctx):
     with pytest.raises(g.GlsError):
         tctx.set_fft_schedule(4096, 4096, 0, 2)       # E=64 does not exist
     with pytest.raises(g.GlsError):
-        tctx.set_fft_schedule(1024, 1024, 5, 0)
+        tctx.set_fft_schedule(1024, 1024, 7, 0)
     with pytest.raises(g.GlsError):
         tctx.set_fft_schedule(1000, 1024, 0, 0)       # not a power of two
 

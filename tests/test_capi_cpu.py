@@ -81,6 +81,7 @@ def test_context_calls_reject_null(native):
     assert native.glsfft_context_set_budget(None, 0) == INVALID
     b = ctypes.c_size_t()
     assert native.glsfft_context_workspace(None, ctypes.byref(b)) == INVALID
+    assert native.glsfft_device_status(None, 0) == INVALID
 
 
 def test_context_create_without_gpu_fails_cleanly(native):
@@ -109,6 +110,8 @@ def test_host_pipeline_and_schedule_calls_reject_bad_arguments(native):
     assert native.glsfft_autotune_fft2d(None, 64, 64, 1, None, None, None, None) == INVALID
     assert native.glsfft_batch_autotune(None, None, 5, None, None, None) == INVALID
     assert native.glsfft_schedule_available(1024, 0, 0) == 1
-    assert native.glsfft_schedule_available(1024, 5, 0) == 0
+    assert native.glsfft_schedule_available(1024, 7, 0) == 0
+    assert native.glsfft_schedule_available(1024, 6, 0) == 0
+    assert native.glsfft_schedule_available(4096, 6, 1) == 1
     assert native.glsfft_schedule_available(1000, 0, 0) == 0
     assert native.glsfft_schedule_available(16, 1, 1) == 0
