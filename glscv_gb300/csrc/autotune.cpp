@@ -102,7 +102,8 @@ int glsfft_set_fft_schedule(glsfft_context ctx, int rows, int cols, int row_sche
     if (!glsfft_schedule_available(cols, row_schedule, 0) ||
         !glsfft_schedule_available(rows, col_schedule, 1))
         return GLSFFT_ERROR_INVALID_VALUE;
-    if (row_schedule == 0 && col_schedule == 0)
+    const FftSchedule d = default_schedule(rows, cols);
+    if (row_schedule == d.row && col_schedule == d.col)
         ctx->sched.erase(sched_key(rows, cols));
     else
         ctx->sched[sched_key(rows, cols)] = FftSchedule{row_schedule, col_schedule};
@@ -114,9 +115,7 @@ int glsfft_get_fft_schedule(glsfft_context ctx, int rows, int cols, int *row_sch
     if (!ctx || !row_schedule || !col_schedule) return GLSFFT_ERROR_INVALID_VALUE;
     const int st = check_dims(rows, cols);
     if (st) return st;
-    FftSchedule sc{};
-    const auto it = ctx->sched.find(sched_key(rows, cols));
-    if (it != ctx->sched.end()) sc = it->second;
+    const FftSchedule sc = schedule_for(ctx->sched, rows, cols);
     *row_schedule = sc.row;
     *col_schedule = sc.col;
     return GLSFFT_SUCCESS;
@@ -172,14 +171,17 @@ int glsfft_autotune_fft2d(glsfft_context ctx, int rows, int cols, int count,
     a.scale = 1.0f;
     a.tw = ctx->d_tw;
     a.in_img_bytes = a.out_img_bytes = (size_t)rows * cols * sizeof(float2);
-    // each pass: its schedules in order, the fastest kept unless schedule 0
-    // is within kKeepMargin of it
+    // each pass: its default schedule first, then the others in order; the
+    // fastest is kept unless the default is within kKeepMargin of it
+    const FftSchedule dflt = default_schedule(rows, cols);
     for (int along_cols = 0; along_cols < 2 && !st; along_cols++) {
         const int n = along_cols ? rows : cols;
+        const int first = along_cols ? dflt.col : dflt.row;
         double best = 0.0, base = 0.0;
-        int best_id = 0;
-        for (int id = 0; id < kPassSchedules && !st; id++) {
-            if (!glsfft_schedule_available(n, id, along_cols)) continue;
+        int best_id = first;
+        for (int k = -1; k < kPassSchedules && !st; k++) {
+            const int id = k < 0 ? first : k;
+            if ((k >= 0 && id == first) || !glsfft_schedule_available(n, id, along_cols)) continue;
             double m = 0.0;
             st = time_median_ms(
                 [&]() {
@@ -188,7 +190,7 @@ int glsfft_autotune_fft2d(glsfft_context ctx, int rows, int cols, int count,
                 },
                 2, 7, s, &m);
             if (st) break;
-            if (id == 0) {
+            if (k < 0) {
                 base = best = m;
             } else if (m < best && m < base * (1.0 - kKeepMargin)) {
                 best = m;

@@ -187,9 +187,7 @@ int glsfft::fft2d_launch(glsfft_context ctx, const void *src, void *dst, int row
     const bool do_rows = cols > 1 || rows == 1 || real_in;
     const bool do_cols = rows > 1;
     const size_t px = (size_t)rows * cols;
-    FftSchedule sc{};
-    const auto it = ctx->sched.find(sched_key(rows, cols));
-    if (it != ctx->sched.end()) sc = it->second;
+    const FftSchedule sc = schedule_for(ctx->sched, rows, cols);
     if (do_rows) {
         PassArgs a{};
         a.in0 = src;
@@ -470,9 +468,7 @@ static int one_pass(glsfft_context ctx, const void *src, void *dst, int count, i
     a.tw = ctx->d_tw;
     a.err = ctx->d_status;
     a.in_img_bytes = a.out_img_bytes = (size_t)rows * cols * sizeof(float2);
-    FftSchedule sc{};
-    const auto it = ctx->sched.find(sched_key(rows, cols));
-    if (it != ctx->sched.end()) sc = it->second;
+    const FftSchedule sc = schedule_for(ctx->sched, rows, cols);
     cudaError_t e = along_rows ? launch_rows_sched(n, sc.row, a, count, s)
                                : launch_cols_sched(n, sc.col, a, count, s);
     return cuda_status(e);

@@ -288,8 +288,9 @@ struct Strided {
 
 // Sm: shared-memory accessor for this thread's line: at(pos) -> float2*
 // (one exchange of complex values, KW as above), or, with Sm::kSplit,
-// at(pos) -> float* (the exchange runs twice through a buffer half the size,
-// real parts then imaginary parts).
+// at<X>(pos) -> float* for the exchange after pass X (the exchange runs
+// twice through a buffer half the size, real parts then imaginary parts;
+// each exchange may pad differently, as its stores and loads are its own).
 // tw: the per-pass twiddle tables above.
 template <int N, int E, class Sync = SyncBlock, int MB = 4>
 struct LineFft {
@@ -397,12 +398,13 @@ struct LineFft {
             const int j = t + s * T;
             const int d = (j / Ns) * Ns * R + (j & (Ns - 1));
 #pragma unroll
-            for (int r = 0; r < R; r++) *sm.at(d + r * Ns) = H ? x[s + r * S].y : x[s + r * S].x;
+            for (int r = 0; r < R; r++)
+                *sm.template at<p>(d + r * Ns) = H ? x[s + r * S].y : x[s + r * S].x;
         }
         sync();
 #pragma unroll
         for (int m = 0; m < E; m++) {
-            const float v = *sm.at(t + m * T);
+            const float v = *sm.template at<p>(t + m * T);
             if constexpr (H == 0) x[m].x = v;
             else x[m].y = v;
         }

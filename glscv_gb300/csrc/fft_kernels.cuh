@@ -47,11 +47,13 @@ struct ColSm {
 // through a float buffer of half the size).  Rows pad one float per 32,
 // columns two per 32: with 16 values per thread and radix-16 passes on
 // 2048- and 4096-point lines these keep the stores and loads of a warp on
-// distinct banks, except the second row exchange's stores (two-way).
+// distinct banks, except the second row exchange's stores (two-way; a
+// second padding for that exchange costs more in registers than it saves).
 struct RowSmF {
     static constexpr bool kSplit = true;
     static constexpr int KW = 1;
     float *base;
+    template <int X>
     __device__ __forceinline__ float *at(int pos) const { return base + pos + (pos >> 5); }
 };
 template <int W>
@@ -60,6 +62,7 @@ struct ColSmF {
     static constexpr int KW = W;
     float *base;
     int c;
+    template <int X>
     __device__ __forceinline__ float *at(int pos) const {
         const int i = pos * W + c;
         return base + i + 2 * (i >> 5);

@@ -160,7 +160,10 @@ GLSFFT_API int glsfft_schedule_available(int length, int schedule, int along_col
 
 /* Pass schedules that glsfft_fft2d_c2c, glsfft_fft2d_batched, the single
  * pass entry points and batch plans' own-launch images use for complex
- * rows x cols images on this context (default 0, 0). */
+ * rows x cols images on this context.  Until set or tuned, a size runs its
+ * built-in default, measured on GB300: row schedule 2 for 2048- and
+ * 4096-point rows, the streamed column pass for 4096-point columns,
+ * schedule 0 otherwise. */
 GLSFFT_API int glsfft_set_fft_schedule(glsfft_context ctx, int rows, int cols, int row_schedule,
                                        int col_schedule);
 GLSFFT_API int glsfft_get_fft_schedule(glsfft_context ctx, int rows, int cols,
@@ -171,12 +174,13 @@ GLSFFT_API int glsfft_get_fft_schedule(glsfft_context ctx, int rows, int cols,
  * schedule of the row pass and of the column pass over `count` images of
  * rows x cols (median of 7 launches after 2, CUDA events on `stream`) on
  * scratch buffers it allocates and frees, and sets the fastest of each
- * (glsfft_set_fft_schedule) unless schedule 0 is within 1% of it.  With
+ * (glsfft_set_fft_schedule) unless the size's default schedule is within
+ * 1% of it.  With
  * cache_path set, the choice is looked up in / appended to that plan cache
  * file (one JSON object per line, keyed by device name, SM count, compute
  * capability, driver, runtime and library versions, rows, cols, count); a
  * hit is applied without timing.  result[3] = {row schedule, column
- * schedule, 1 if from the cache}; ms[2] = {chosen, schedule 0}: row plus
+ * schedule, 1 if from the cache}; ms[2] = {chosen, default}: row plus
  * column pass time of one launch each.  Either may be NULL.
  */
 GLSFFT_API int glsfft_autotune_fft2d(glsfft_context ctx, int rows, int cols, int count,

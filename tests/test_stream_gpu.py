@@ -118,3 +118,23 @@ def test_streamed_schedule_availability(native):
     for n in (64, 1024):
         assert not g.schedule_available(n, STREAMED, False)
         assert not g.schedule_available(n, STREAMED, True)
+
+
+def test_builtin_default_schedules(tctx, torch_cuda):
+    # a fresh context: 4096^2 runs row schedule 2 and the streamed column
+    # pass, 2048-point rows schedule 2, other sizes schedule 0
+    assert tctx.get_fft_schedule(4096, 4096) == (2, STREAMED)
+    assert tctx.get_fft_schedule(2048, 2048) == (2, 0)
+    assert tctx.get_fft_schedule(1024, 1024) == (0, 0)
+    assert tctx.get_fft_schedule(4096, 1024) == (0, STREAMED)
+    x = wl.complex_uniform(4096, 4096, 1330)
+    s = stream_handle(torch_cuda)
+    d = torch_cuda.from_numpy(x).cuda()
+    y = torch_cuda.empty_like(d)
+    tctx.fft2d(d.data_ptr(), y.data_ptr(), 4096, 4096, 0, s)       # the defaults
+    torch_cuda.cuda.synchronize()
+    ref = _run(tctx, torch_cuda, x, 4096, 4096, 0, 1, (0, 0))       # explicit schedule 0
+    assert tctx.get_fft_schedule(4096, 4096) == (0, 0)
+    assert np.array_equal(ref.view(np.uint32), y.cpu().numpy().view(np.uint32))
+    tctx.set_fft_schedule(4096, 4096, 2, STREAMED)                  # back to the default
+    assert tctx.get_fft_schedule(4096, 4096) == (2, STREAMED)
