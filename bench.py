@@ -62,6 +62,9 @@ def parse():
                    help="run only the serving sweep and print its JSON")
     p.add_argument("--profile-spectrum", action="store_true",
                    help="run each spectrum operation once on 4096x4096 and exit (for ncu)")
+    p.add_argument("--profile-fft", type=int, default=0, metavar="N",
+                   help="run gls::fft forward on one NxN image three times with the size's "
+                        "default pass schedules and exit (for ncu)")
     return p.parse_args()
 
 
@@ -640,6 +643,19 @@ def run_own(args) -> None:
 
     if args.serving_only:
         print(json.dumps(serving_sweep(g, ctx, torch, slots=args.serve_slots)), flush=True)
+        ctx.close()
+        return
+
+    if args.profile_fft:
+        # the plain path on one image: three forward transforms, for ncu
+        n = args.profile_fft
+        x = torch.from_numpy(wl.complex_uniform(n, n, 2)).cuda()
+        y = torch.empty_like(x)
+        for _ in range(3):
+            ctx.fft2d(x.data_ptr(), y.data_ptr(), n, n, 0, s)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_fft": n, "schedule": list(ctx.get_fft_schedule(n, n)),
+                          "device_status": ctx.device_status()}), flush=True)
         ctx.close()
         return
 
