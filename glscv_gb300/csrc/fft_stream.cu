@@ -83,10 +83,15 @@ __host__ __device__ constexpr int stream_threads() {
     return stream_lines<N>() * (N / E);
 }
 
-template <int N, int E, bool COLS>
+// ST: ST_C2 (complex out), or, for a column pass over one image,
+// ST_LOGMAG_MINMAX (the FFT display epilogue of the plain column kernel:
+// log(|X| + param) as CV_32FC1 and the minMaxLoc keys of what is stored,
+// reduced over all of the block's tiles and committed once)
+template <int N, int E, bool COLS, int ST>
 __global__ void __launch_bounds__(stream_threads<N, E>(), 1)
     fft_stream_kernel(const __grid_constant__ CUtensorMap tmap, const PassArgs a, int images) {
     constexpr int L = stream_lines<N>(), T = N / E;
+    static_assert(ST == ST_C2 || (COLS && ST == ST_LOGMAG_MINMAX), "stream store modes");
     static_assert(N % 256 == 0, "column tiles are read as 256-row boxes");
     extern __shared__ unsigned char stream_raw[];
     // 128-byte aligned stage; offsetting the shared array itself (not a cast
@@ -112,6 +117,7 @@ __global__ void __launch_bounds__(stream_threads<N, E>(), 1)
     int tile = blockIdx.x;
     if (tid == 0 && tile < total) stream_issue<N, COLS>(&tmap, a, tile, tpi, stage, full);
     unsigned parity = 0;
+    MinMaxAny run;  // ST_LOGMAG_MINMAX only
     for (; tile < total; tile += gridDim.x) {
         const bool ok = mbar_wait(full, parity, kStreamWaitNs);
         if (__syncthreads_or(!ok)) {
@@ -142,7 +148,20 @@ __global__ void __launch_bounds__(stream_threads<N, E>(), 1)
         const int img = tile / tpi, j = tile % tpi;
         float2 *out = reinterpret_cast<float2 *>(static_cast<char *>(a.out0) +
                                                  (size_t)img * a.out_img_bytes);
-        if constexpr (COLS) {
+        if constexpr (ST == ST_LOGMAG_MINMAX) {
+            const int col = j * L + l;
+            const int ocol = (a.flags & PF_SHIFT_COLS) ? (col + (a.cols >> 1)) & (a.cols - 1) : col;
+            float *fo = reinterpret_cast<float *>(out);
+#pragma unroll
+            for (int m = 0; m < E; m++) {
+                const int pos = t + m * T;
+                const int orow = (a.flags & PF_SHIFT_ROWS) ? (pos + (N >> 1)) & (N - 1) : pos;
+                const unsigned o = (unsigned)orow * (unsigned)a.cols + (unsigned)ocol;
+                const float v = spec_log_mag(x[m], a.param);
+                fo[o] = v;
+                run.add(v, o);
+            }
+        } else if constexpr (COLS) {
             const int col = j * L + l;
             const int ocol = (a.flags & PF_SHIFT_COLS) ? (col + (a.cols >> 1)) & (a.cols - 1) : col;
             store_line<N, E, T>(out + ocol, (size_t)a.cols, x, t, a.flags & PF_SHIFT_ROWS);
@@ -151,6 +170,10 @@ __global__ void __launch_bounds__(stream_threads<N, E>(), 1)
             const int orow = (a.flags & PF_SHIFT_ROWS) ? (row + (a.rows >> 1)) & (a.rows - 1) : row;
             store_line<N, E, T>(out + (size_t)orow * N, 1, x, t, a.flags & PF_SHIFT_COLS);
         }
+    }
+    if constexpr (ST == ST_LOGMAG_MINMAX) {
+        __shared__ unsigned long long red[2 * (stream_threads<N, E>() / 32)];
+        block_minmax_commit(run.kmin(), run.kmax(), red, a.key);
     }
 }
 
@@ -168,7 +191,7 @@ int sm_count(int device) {
     return cached[device];
 }
 
-template <int N, int E, bool COLS>
+template <int N, int E, bool COLS, int ST = ST_C2>
 cudaError_t stream_launch(const PassArgs &a, int images, cudaStream_t s) {
     constexpr int L = stream_lines<N>();
     CUtensorMap tmap{};
@@ -177,7 +200,7 @@ cudaError_t stream_launch(const PassArgs &a, int images, cudaStream_t s) {
             return cudaErrorNotSupported;
     }
     constexpr size_t smem = stream_smem<N, COLS>();
-    auto kern = fft_stream_kernel<N, E, COLS>;
+    auto kern = fft_stream_kernel<N, E, COLS, ST>;
     static cudaError_t once =
         cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (once != cudaSuccess) return once;
@@ -194,20 +217,25 @@ cudaError_t stream_launch(const PassArgs &a, int images, cudaStream_t s) {
 
 }  // namespace
 
-bool stream_pass_applies(int n, bool cols, const PassArgs &a, int images) {
+bool stream_pass_applies(int n, bool cols, const PassArgs &a, int images, int st) {
     if (n != 2048 && n != 4096) return false;
     if (a.in1 || a.out1 || !a.in0 || !a.out0 || images < 1) return false;
+    if (st != ST_C2 && !(st == ST_LOGMAG_MINMAX && cols && images == 1 && a.key)) return false;
     const int L = (int)(kStreamTileBytes / (n * sizeof(float2)));
     const int other = cols ? a.cols : a.rows;  // lines in the pass
     if ((cols ? a.rows : a.cols) != n || other < L || other % L) return false;
     const size_t img = (size_t)a.rows * a.cols * sizeof(float2);
-    if (a.in_img_bytes != img || a.out_img_bytes != img) return false;
+    if (images > 1 && (a.in_img_bytes != img || a.out_img_bytes != img)) return false;
     const uintptr_t in = reinterpret_cast<uintptr_t>(a.in0), out = reinterpret_cast<uintptr_t>(a.out0);
-    return (in % 16) == 0 && (out % 16) == 0;
+    return (in % 16) == 0 && (out % (st == ST_C2 ? 16 : 4)) == 0;
 }
 
-cudaError_t launch_stream_pass(int n, bool cols, const PassArgs &a, int images, cudaStream_t s) {
-    if (!stream_pass_applies(n, cols, a, images)) return cudaErrorNotSupported;
+cudaError_t launch_stream_pass(int n, bool cols, const PassArgs &a, int images, cudaStream_t s,
+                               int st) {
+    if (!stream_pass_applies(n, cols, a, images, st)) return cudaErrorNotSupported;
+    if (st == ST_LOGMAG_MINMAX)
+        return n == 2048 ? stream_launch<2048, 16, true, ST_LOGMAG_MINMAX>(a, images, s)
+                         : stream_launch<4096, 16, true, ST_LOGMAG_MINMAX>(a, images, s);
     // 16 values per thread (1024 threads); 32 per thread (512 threads)
     // measured the same on GB300
     if (n == 2048) return cols ? stream_launch<2048, 16, true>(a, images, s) : stream_launch<2048, 16, false>(a, images, s);

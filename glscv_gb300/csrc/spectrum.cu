@@ -42,8 +42,9 @@ int grid_for(size_t n, int per_sm = 8) {
 
 // The element kernels move 16 bytes per load and store (two complex or four
 // float values per step; a scalar loop covers a misaligned or odd tail) and
-// keep two steps in flight per thread, so a grid of eight resident blocks
-// per SM streams at HBM rate.
+// issue the loads of two steps (four for the float-input kernels) before
+// using them, so each thread keeps several loads in flight and a grid of
+// eight resident blocks per SM streams at HBM rate.
 __device__ __forceinline__ bool al16(const void *p) {
     return (reinterpret_cast<uintptr_t>(p) & 15) == 0;
 }
@@ -64,13 +65,18 @@ __global__ void __launch_bounds__(kThreads) spec_binary_kernel(const float2 *a, 
         const float4 *a4 = reinterpret_cast<const float4 *>(a);
         const float4 *b4 = reinterpret_cast<const float4 *>(b);
         float4 *d4 = reinterpret_cast<float4 *>(d);
-#pragma unroll 2
-        for (size_t i = tid; i < nv; i += stride) {
-            const float4 x = a4[i], y = b4[i];
+        auto step = [&](const float4 x, const float4 y) {
             const float2 r0 = spec_binary_op<OP>(make_float2(x.x, x.y), make_float2(y.x, y.y));
             const float2 r1 = spec_binary_op<OP>(make_float2(x.z, x.w), make_float2(y.z, y.w));
-            d4[i] = make_float4(r0.x, r0.y, r1.x, r1.y);
+            return make_float4(r0.x, r0.y, r1.x, r1.y);
+        };
+        size_t i = tid;
+        for (; i + stride < nv; i += 2 * stride) {  // both steps' loads in flight
+            const float4 x0 = a4[i], y0 = b4[i], x1 = a4[i + stride], y1 = b4[i + stride];
+            d4[i] = step(x0, y0);
+            d4[i + stride] = step(x1, y1);
         }
+        if (i < nv) d4[i] = step(a4[i], b4[i]);
         done = nv * 2;
     }
     for (size_t i = done + tid; i < n; i += stride) d[i] = spec_binary_op<OP>(a[i], b[i]);
@@ -102,9 +108,7 @@ __global__ void __launch_bounds__(kThreads) spec_mag_kernel(const float2 *__rest
         const size_t nv = n / 4;
         const float4 *a4 = reinterpret_cast<const float4 *>(a);
         float4 *d4 = reinterpret_cast<float4 *>(d);
-#pragma unroll 2
-        for (size_t i = tid; i < nv; i += stride) {
-            const float4 p = a4[2 * i], q = a4[2 * i + 1];
+        auto step = [&](size_t i, const float4 p, const float4 q) {
             const float4 r = make_float4(mag_op<LOG>(make_float2(p.x, p.y), offset),
                                          mag_op<LOG>(make_float2(p.z, p.w), offset),
                                          mag_op<LOG>(make_float2(q.x, q.y), offset),
@@ -116,7 +120,15 @@ __global__ void __launch_bounds__(kThreads) spec_mag_kernel(const float2 *__rest
                 keys_add(r.z, 4 * i + 2, kmin, kmax);
                 keys_add(r.w, 4 * i + 3, kmin, kmax);
             }
+        };
+        size_t i = tid;
+        for (; i + stride < nv; i += 2 * stride) {  // both steps' loads in flight
+            const float4 p0 = a4[2 * i], q0 = a4[2 * i + 1];
+            const float4 p1 = a4[2 * (i + stride)], q1 = a4[2 * (i + stride) + 1];
+            step(i, p0, q0);
+            step(i + stride, p1, q1);
         }
+        if (i < nv) step(i, a4[2 * i], a4[2 * i + 1]);
         done = nv * 4;
     }
     for (size_t i = done + tid; i < n; i += stride) {
@@ -159,8 +171,23 @@ __global__ void __launch_bounds__(kThreads) minmax_kernel(const float *__restric
     if (al16(x)) {
         const size_t nv = n / 4;
         const float4 *x4 = reinterpret_cast<const float4 *>(x);
-#pragma unroll 4
-        for (size_t i = tid; i < nv; i += stride) {
+        // four independent 16-byte loads in flight before the compares (the
+        // visiting order per thread stays increasing)
+        size_t i = tid;
+        for (; i + 3 * stride < nv; i += 4 * stride) {
+            float4 v[4];
+#pragma unroll
+            for (int k = 0; k < 4; k++) v[k] = x4[i + k * stride];
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                const unsigned b = (unsigned)(4 * (i + k * stride));
+                run.add(v[k].x, b);
+                run.add(v[k].y, b + 1);
+                run.add(v[k].z, b + 2);
+                run.add(v[k].w, b + 3);
+            }
+        }
+        for (; i < nv; i += stride) {
             const float4 v = x4[i];
             run.add(v.x, (unsigned)(4 * i));
             run.add(v.y, (unsigned)(4 * i + 1));
@@ -187,12 +214,19 @@ __global__ void __launch_bounds__(kThreads) normalize_kernel(const float *x, flo
         const size_t nv = n / 4;
         const float4 *x4 = reinterpret_cast<const float4 *>(x);
         float4 *d4 = reinterpret_cast<float4 *>(d);
-#pragma unroll 2
-        for (size_t i = tid; i < nv; i += stride) {
-            const float4 v = x4[i];
-            d4[i] = make_float4(__fadd_rn(c, __fmul_rn(scl, v.x)), __fadd_rn(c, __fmul_rn(scl, v.y)),
-                                __fadd_rn(c, __fmul_rn(scl, v.z)), __fadd_rn(c, __fmul_rn(scl, v.w)));
+        auto step = [&](const float4 v) {
+            return make_float4(__fadd_rn(c, __fmul_rn(scl, v.x)), __fadd_rn(c, __fmul_rn(scl, v.y)),
+                               __fadd_rn(c, __fmul_rn(scl, v.z)), __fadd_rn(c, __fmul_rn(scl, v.w)));
+        };
+        size_t i = tid;
+        for (; i + 3 * stride < nv; i += 4 * stride) {  // four loads in flight
+            float4 v[4];
+#pragma unroll
+            for (int k = 0; k < 4; k++) v[k] = x4[i + k * stride];
+#pragma unroll
+            for (int k = 0; k < 4; k++) d4[i + k * stride] = step(v[k]);
         }
+        for (; i < nv; i += stride) d4[i] = step(x4[i]);
         done = nv * 4;
     }
     for (size_t i = done + tid; i < n; i += stride) d[i] = __fadd_rn(c, __fmul_rn(scl, x[i]));
@@ -390,7 +424,11 @@ int glsfft_fft_display(glsfft_context ctx, const float *frame, const float *wind
         c.key = keys;
         c.tw = ctx->d_tw;
         c.param = offset;
-        e = launch_cols(rows, LD_C2, ST_LOGMAG_MINMAX, c, 1, s);
+        c.err = ctx->d_status;
+        // 4096-point columns: the streamed pass (TMA-fed, one block per SM)
+        e = rows == 4096 && stream_pass_applies(rows, true, c, 1, ST_LOGMAG_MINMAX)
+                ? launch_stream_pass(rows, true, c, 1, s, ST_LOGMAG_MINMAX)
+                : launch_cols(rows, LD_C2, ST_LOGMAG_MINMAX, c, 1, s);
     } else {
         spec_mag_kernel<true, true><<<grid_for(n), kThreads, 0, s>>>(spec, dst, n, offset, keys);
         e = cudaGetLastError();

@@ -159,3 +159,28 @@ def test_fft_display_pipeline(ctx, torch_cuda, oracle, shape, window):
     # the brightest bin is the DC term, at the centre after the shift
     if rows > 1:
         assert np.unravel_index(np.argmax(got), got.shape) == (rows // 2, cols // 2)
+
+
+def test_fft_display_4096_equals_composed_ops(ctx, torch_cuda):
+    # 4096-point columns run the streamed column pass with the log-magnitude
+    # epilogue; the fused pipeline must equal the same steps as separate
+    # calls bit for bit: window * frame, gls::fft(SHIFT) of the promoted
+    # product, logMagSpectrums(1), normalize(0, 1, NORM_MINMAX)
+    torch = torch_cuda
+    s = stream_handle(torch)
+    n = 4096
+    frame = wl.smooth_field(n, n, seed=23)
+    win = wl.hann_window(n, n)
+    df, dw = _dev(torch, frame), _dev(torch, win)
+    fused = torch.empty((n, n), dtype=torch.float32, device="cuda")
+    ctx.fft_display(df.data_ptr(), dw.data_ptr(), fused.data_ptr(), n, n, 1.0, s)
+    prod = _dev(torch, (frame * win).astype(np.float32))
+    spec = torch.empty((n, n), dtype=torch.complex64, device="cuda")
+    ctx.fft2d(prod.data_ptr(), spec.data_ptr(), n, n, 64, s, real_input=True)
+    lm = torch.empty((n, n), dtype=torch.float32, device="cuda")
+    ctx.log_mag_spectrums(spec.data_ptr(), lm.data_ptr(), n, n, 1.0, s)
+    composed = torch.empty_like(lm)
+    ctx.normalize_minmax(lm.data_ptr(), composed.data_ptr(), n, n, 0.0, 1.0, s)
+    torch.cuda.synchronize()
+    assert _eq(fused.cpu().numpy(), composed.cpu().numpy())
+    assert ctx.device_status() == 0
