@@ -28,13 +28,20 @@ namespace {
 
 constexpr int kThreads = 256;
 
-// blocks for n elements: per_sm resident blocks per SM at most (grid-stride
-// beyond); reductions use fewer, longer blocks to keep the per-block atomics few
-int grid_for(size_t n, int per_sm = 8) {
-    int dev = 0, sms = 0;
+// Blocks for n elements: one wave of the kernel's resident blocks at most
+// (grid-stride beyond).  A grid of more blocks than fit at once would run a
+// partial second wave at a fraction of the occupancy.
+template <class Kernel>
+int grid_for(Kernel kern, size_t n) {
+    int dev = 0, sms = 0, per_sm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreads, 0) != cudaSuccess) {
+        cudaGetLastError();
+        per_sm = 1;
+    }
     if (sms <= 0) sms = 1;
+    if (per_sm <= 0) per_sm = 1;
     const size_t want = (n + kThreads - 1) / kThreads;
     const size_t cap = (size_t)sms * per_sm;
     return (int)(want < cap ? (want ? want : 1) : cap);
@@ -171,15 +178,17 @@ __global__ void __launch_bounds__(kThreads) minmax_kernel(const float *__restric
     if (al16(x)) {
         const size_t nv = n / 4;
         const float4 *x4 = reinterpret_cast<const float4 *>(x);
-        // four independent 16-byte loads in flight before the compares (the
-        // visiting order per thread stays increasing)
+        // eight independent 16-byte loads in flight before the compares (a
+        // read-only stream needs more bytes in flight per thread than a copy;
+        // the visiting order per thread stays increasing)
+        constexpr int kBatch = 8;
         size_t i = tid;
-        for (; i + 3 * stride < nv; i += 4 * stride) {
-            float4 v[4];
+        for (; i + (kBatch - 1) * stride < nv; i += kBatch * stride) {
+            float4 v[kBatch];
 #pragma unroll
-            for (int k = 0; k < 4; k++) v[k] = x4[i + k * stride];
+            for (int k = 0; k < kBatch; k++) v[k] = x4[i + k * stride];
 #pragma unroll
-            for (int k = 0; k < 4; k++) {
+            for (int k = 0; k < kBatch; k++) {
                 const unsigned b = (unsigned)(4 * (i + k * stride));
                 run.add(v[k].x, b);
                 run.add(v[k].y, b + 1);
@@ -271,8 +280,11 @@ int glsfft_mul_spectrums(glsfft_context ctx, const void *src0, const void *src1,
     const auto *a = static_cast<const float2 *>(src0);
     const auto *b = static_cast<const float2 *>(src1);
     auto *d = static_cast<float2 *>(dst);
-    if (conj) spec_binary_kernel<1><<<grid_for(n), kThreads, 0, (cudaStream_t)stream>>>(a, b, d, n);
-    else spec_binary_kernel<0><<<grid_for(n), kThreads, 0, (cudaStream_t)stream>>>(a, b, d, n);
+    cudaStream_t s = (cudaStream_t)stream;
+    if (conj)
+        spec_binary_kernel<1><<<grid_for(spec_binary_kernel<1>, n), kThreads, 0, s>>>(a, b, d, n);
+    else
+        spec_binary_kernel<0><<<grid_for(spec_binary_kernel<0>, n), kThreads, 0, s>>>(a, b, d, n);
     return cuda_status(cudaGetLastError());
 }
 
@@ -284,7 +296,8 @@ int glsfft_mul_spectrums_phase_only(glsfft_context ctx, const void *src0, const 
     DeviceGuard g(ctx->device);
     if (!g.ok()) return GLSFFT_ERROR_CUDA;
     const size_t n = (size_t)rows * cols;
-    spec_binary_kernel<2><<<grid_for(n), kThreads, 0, (cudaStream_t)stream>>>(
+    auto kern = spec_binary_kernel<2>;
+    kern<<<grid_for(kern, n), kThreads, 0, (cudaStream_t)stream>>>(
         static_cast<const float2 *>(src0), static_cast<const float2 *>(src1),
         static_cast<float2 *>(dst), n);
     return cuda_status(cudaGetLastError());
@@ -301,7 +314,8 @@ int glsfft_mag_spectrums(glsfft_context ctx, const void *src, float *dst, int ro
     DeviceGuard g(ctx->device);
     if (!g.ok()) return GLSFFT_ERROR_CUDA;
     const size_t n = (size_t)rows * cols;
-    spec_mag_kernel<false, false><<<grid_for(n), kThreads, 0, (cudaStream_t)stream>>>(
+    auto kern = spec_mag_kernel<false, false>;
+    kern<<<grid_for(kern, n), kThreads, 0, (cudaStream_t)stream>>>(
         static_cast<const float2 *>(src), dst, n, 0.0f, nullptr);
     return cuda_status(cudaGetLastError());
 }
@@ -316,7 +330,8 @@ int glsfft_log_mag_spectrums(glsfft_context ctx, const void *src, float *dst, in
     DeviceGuard g(ctx->device);
     if (!g.ok()) return GLSFFT_ERROR_CUDA;
     const size_t n = (size_t)rows * cols;
-    spec_mag_kernel<true, false><<<grid_for(n), kThreads, 0, (cudaStream_t)stream>>>(
+    auto kern = spec_mag_kernel<true, false>;
+    kern<<<grid_for(kern, n), kThreads, 0, (cudaStream_t)stream>>>(
         static_cast<const float2 *>(src), dst, n, offset, nullptr);
     return cuda_status(cudaGetLastError());
 }
@@ -331,7 +346,8 @@ int glsfft_min_max_loc_async(glsfft_context ctx, const float *src, int rows, int
     const size_t n = (size_t)rows * cols;
     cudaError_t e = cudaMemsetAsync(d_keys, 0, 2 * sizeof(unsigned long long), (cudaStream_t)stream);
     if (e != cudaSuccess) return cuda_status(e);
-    minmax_kernel<<<grid_for(n / 4, 8), kThreads, 0, (cudaStream_t)stream>>>(src, n, d_keys);
+    minmax_kernel<<<grid_for(minmax_kernel, n / 4), kThreads, 0, (cudaStream_t)stream>>>(src, n,
+                                                                                         d_keys);
     return cuda_status(cudaGetLastError());
 }
 
@@ -377,8 +393,8 @@ int glsfft_normalize_minmax(glsfft_context ctx, const float *src, float *dst, in
     if (!st) st = glsfft_min_max_loc_async(ctx, src, rows, cols, keys, stream);
     if (st) return st;
     const size_t n = (size_t)rows * cols;
-    normalize_kernel<<<grid_for(n), kThreads, 0, (cudaStream_t)stream>>>(src, dst, n, keys, alpha,
-                                                                         beta);
+    normalize_kernel<<<grid_for(normalize_kernel, n), kThreads, 0, (cudaStream_t)stream>>>(
+        src, dst, n, keys, alpha, beta);
     return cuda_status(cudaGetLastError());
 }
 
@@ -430,12 +446,13 @@ int glsfft_fft_display(glsfft_context ctx, const float *frame, const float *wind
                 ? launch_stream_pass(rows, true, c, 1, s, ST_LOGMAG_MINMAX)
                 : launch_cols(rows, LD_C2, ST_LOGMAG_MINMAX, c, 1, s);
     } else {
-        spec_mag_kernel<true, true><<<grid_for(n), kThreads, 0, s>>>(spec, dst, n, offset, keys);
+        auto kern = spec_mag_kernel<true, true>;
+        kern<<<grid_for(kern, n), kThreads, 0, s>>>(spec, dst, n, offset, keys);
         e = cudaGetLastError();
     }
     if (e != cudaSuccess) return cuda_status(e);
     // normalize(0, 1, NORM_MINMAX) in place
-    normalize_kernel<<<grid_for(n), kThreads, 0, s>>>(dst, dst, n, keys, 0.0, 1.0);
+    normalize_kernel<<<grid_for(normalize_kernel, n), kThreads, 0, s>>>(dst, dst, n, keys, 0.0, 1.0);
     return cuda_status(cudaGetLastError());
 }
 
