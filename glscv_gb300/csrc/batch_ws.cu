@@ -468,9 +468,7 @@ __global__ void __launch_bounds__(kBlock, MINB) fft_batch_ws(BatchArgs a) {
 // 3 -> (3, 2) (three blocks fit the SM's shared memory only with two stages).
 template <int MINB, int ST>
 static cudaError_t prepare_ws() {
-    static cudaError_t once = cudaFuncSetAttribute(
-        fft_batch_ws<MINB, ST>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ws_smem<ST>());
-    return once;
+    return smem_opt_in(reinterpret_cast<const void *>(fft_batch_ws<MINB, ST>), ws_smem<ST>());
 }
 
 template <int MINB, int ST>

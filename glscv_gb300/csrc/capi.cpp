@@ -7,6 +7,8 @@
 #include <cstdint>
 #include <cstring>
 #include <mutex>
+#include <set>
+#include <utility>
 #include <new>
 #include <vector>
 
@@ -156,6 +158,19 @@ DeviceGuard::DeviceGuard(int dev) {
 DeviceGuard::~DeviceGuard() {
     int cur = -1;
     if (prev_ >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev_) cudaSetDevice(prev_);
+}
+
+cudaError_t glsfft::smem_opt_in(const void *kern, size_t bytes) {
+    static std::mutex mu;
+    static std::set<std::pair<const void *, int>> done;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lock(mu);
+    if (done.count({kern, dev})) return cudaSuccess;
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e == cudaSuccess) done.insert({kern, dev});
+    return e;
 }
 
 int glsfft::ensure_workspace(glsfft_context ctx, size_t bytes) {

@@ -11,8 +11,8 @@ static cudaError_t rows_t(const PassArgs &a, int images, cudaStream_t s) {
     constexpr size_t smem = num_passes(N) > 1 ? sizeof(float2) * (size_t)LINES * padded_count(N) : 0;
     auto kern = fft_rows_kernel<N, E, LINES, LD, ST>;
     if constexpr (smem > 48 * 1024) {
-        static cudaError_t once = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (once != cudaSuccess) return once;
+        const cudaError_t e = smem_opt_in(reinterpret_cast<const void *>(kern), smem);
+        if (e != cudaSuccess) return e;
     }
     dim3 grid((a.rows + LINES - 1) / LINES, images);
     kern<<<grid, threads, smem, s>>>(a);

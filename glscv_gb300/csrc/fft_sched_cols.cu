@@ -16,9 +16,8 @@ static cudaError_t cols_s(const PassArgs &a, int images, cudaStream_t s) {
         constexpr size_t smem = (size_t)shape_smem(N, sh, true);
         auto kern = fft_cols_kernel<N, sh.E, sh.G, LD_C2, ST_C2, sh.MB>;
         if constexpr (smem > 48 * 1024) {
-            static cudaError_t once =
-                cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            if (once != cudaSuccess) return once;
+            const cudaError_t e = smem_opt_in(reinterpret_cast<const void *>(kern), smem);
+            if (e != cudaSuccess) return e;
         }
         dim3 grid((a.cols + sh.G - 1) / sh.G, images);
         kern<<<grid, threads, smem, s>>>(a);

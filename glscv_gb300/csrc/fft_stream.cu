@@ -178,17 +178,12 @@ __global__ void __launch_bounds__(stream_threads<N, E>(), 1)
 }
 
 int sm_count(int device) {
-    static int cached[64] = {0};
-    if (device < 0 || device >= 64) return 0;
-    if (!cached[device]) {
-        int v = 0;
-        if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) {
-            cudaGetLastError();
-            return 0;
-        }
-        cached[device] = v;
+    int v = 0;
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
     }
-    return cached[device];
+    return v;
 }
 
 template <int N, int E, bool COLS, int ST = ST_C2>
@@ -201,11 +196,10 @@ cudaError_t stream_launch(const PassArgs &a, int images, cudaStream_t s) {
     }
     constexpr size_t smem = stream_smem<N, COLS>();
     auto kern = fft_stream_kernel<N, E, COLS, ST>;
-    static cudaError_t once =
-        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (once != cudaSuccess) return once;
+    cudaError_t e = smem_opt_in(reinterpret_cast<const void *>(kern), smem);
+    if (e != cudaSuccess) return e;
     int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
+    e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
     const int sms = sm_count(dev);
     if (sms <= 0) return cudaErrorNotSupported;

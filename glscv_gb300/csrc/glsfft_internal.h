@@ -82,6 +82,11 @@ cudaError_t launch_stream_pass(int n, bool cols, const PassArgs &a, int images, 
 int make_tmap_2d(void *tmap128, const void *base, long long width, long long height, int box_w,
                  int box_h);
 
+// Opt kernel `kern` into `bytes` of dynamic shared memory on the current
+// device.  The attribute belongs to the kernel's instance on one device, so
+// this runs once per (kernel, device) (thread-safe; capi.cpp).
+cudaError_t smem_opt_in(const void *kern, size_t bytes);
+
 // Twiddle tables: one device buffer of kTwEntries float2 holding the
 // per-pass tables of fft_device.cuh (tw_offset).  Generated in FP64 on the
 // host and rounded once to FP32.

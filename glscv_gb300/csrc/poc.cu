@@ -12,8 +12,8 @@ static cudaError_t poc_t(const PassArgs &a, cudaStream_t s) {
     constexpr size_t smem = num_passes(N) > 1 ? sizeof(float2) * (size_t)padded_count(N * W) : 0;
     auto kern = poc_cols_kernel<N, E, W>;
     if constexpr (smem > 48 * 1024) {
-        static cudaError_t once = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (once != cudaSuccess) return once;
+        const cudaError_t e = smem_opt_in(reinterpret_cast<const void *>(kern), smem);
+        if (e != cudaSuccess) return e;
     }
     dim3 grid((a.cols + W - 1) / W, 1);
     kern<<<grid, threads, smem, s>>>(a);

@@ -231,9 +231,8 @@ template <int N1, bool ROWS>
 cudaError_t tc_launch(const PassArgs &a, const TcTables &t, int images, cudaStream_t s) {
     using Lay = TcLayout<N1>;
     auto kern = tc_lines_kernel<N1, ROWS>;
-    static cudaError_t once =
-        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Lay::SMEM);
-    if (once != cudaSuccess) return once;
+    const cudaError_t e = smem_opt_in(reinterpret_cast<const void *>(kern), Lay::SMEM);
+    if (e != cudaSuccess) return e;
     const int nlines = ROWS ? a.rows : a.cols;
     dim3 grid((nlines + Lay::L - 1) / Lay::L, images);
     const __half *fh = N1 == 32 ? t.f32_hi : t.f64_hi;
