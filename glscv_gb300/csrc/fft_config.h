@@ -42,9 +42,10 @@ __host__ __device__ constexpr int padded_count(int count) { return count + (coun
 //   4: twice the lines or columns per block
 //   5: 1 and 3 together (half the elements per thread, half the lines or
 //      columns per block: smaller blocks, more of them resident per SM)
-//   6: streamed (fft_stream.cu): one persistent block per SM that copies
-//      the next 128 KB tile in with the TMA while it transforms the current
-//      one; 2048- and 4096-point lines only, bit-identical to schedule 0
+//   6: streamed column pass (fft_stream.cu): one persistent block per SM
+//      that copies the next 128 KB tile in with the TMA while it transforms
+//      the current one; 2048- and 4096-point columns only, bit-identical to
+//      schedule 0
 // Schedules 1..5 exist for N >= kSchedMinLen when the block has 32..1024
 // threads, fits 227 KB of shared memory and its E divides N; every
 // schedule computes the same transform (the rounding differs with the radix
@@ -92,7 +93,7 @@ __host__ __device__ constexpr bool same_shape(PassShape a, PassShape b) {
 // whether schedule `id` of a row (cols=false) or column pass of length n
 // exists and differs from schedule 0
 __host__ __device__ constexpr bool sched_available(int n, int id, bool cols) {
-    return id == 0 || (id == kSchedStreamed && (n == 2048 || n == 4096)) ||
+    return id == 0 || (id == kSchedStreamed && cols && (n == 2048 || n == 4096)) ||
            (id > 0 && id < kSchedStreamed && n >= kSchedMinLen && n <= 4096 &&
             shape_ok(n, cols ? col_shape(n, id) : row_shape(n, id), cols) &&
             !same_shape(cols ? col_shape(n, id) : row_shape(n, id),

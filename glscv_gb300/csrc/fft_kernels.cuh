@@ -43,19 +43,11 @@ struct ColSm {
     }
 };
 
-// Split-exchange accessors (real and imaginary parts exchanged in turn
-// through a float buffer of half the size).  Rows pad one float per 32,
-// columns two per 32: with 16 values per thread and radix-16 passes on
-// 2048- and 4096-point lines these keep the stores and loads of a warp on
-// distinct banks, except the second row exchange's stores (two-way; a
-// second padding for that exchange costs more in registers than it saves).
-struct RowSmF {
-    static constexpr bool kSplit = true;
-    static constexpr int KW = 1;
-    float *base;
-    template <int X>
-    __device__ __forceinline__ float *at(int pos) const { return base + pos + (pos >> 5); }
-};
+// Split-exchange accessor for a column tile (real and imaginary parts
+// exchanged in turn through a float buffer of half the size), two pad floats
+// per 32: with 16 values per thread and radix-16 passes on 2048- and
+// 4096-point columns of 8 or 4 per tile, the stores and loads of a warp fall
+// on distinct banks.
 template <int W>
 struct ColSmF {
     static constexpr bool kSplit = true;
@@ -68,7 +60,6 @@ struct ColSmF {
         return base + i + 2 * (i >> 5);
     }
 };
-__host__ __device__ constexpr int row_split_floats(int n) { return n + (n >> 5); }
 __host__ __device__ constexpr int col_split_floats(int count) { return count + 2 * (count >> 5); }
 
 // Whole-line conjugation and scaling behind uniform branches, so the common

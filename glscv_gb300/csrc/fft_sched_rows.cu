@@ -47,11 +47,6 @@ cudaError_t launch_rows_sched(int n, int id, const PassArgs &a, int images, cuda
     case 3: return rows_id<3>(n, a, images, s);
     case 4: return rows_id<4>(n, a, images, s);
     case 5: return rows_id<5>(n, a, images, s);
-    case kSchedStreamed: {
-        // arguments the streamed pass does not take run schedule 0
-        if (!stream_pass_applies(n, false, a, images)) return launch_rows(n, LD_C2, ST_C2, a, images, s);
-        return launch_stream_pass(n, false, a, images, s);
-    }
     default: return cudaErrorInvalidValue;
     }
 }

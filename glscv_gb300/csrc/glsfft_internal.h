@@ -67,11 +67,11 @@ cudaError_t launch_rows(int n, int ld, int st, const PassArgs &a, int images, cu
 cudaError_t launch_cols(int n, int ld, int st, const PassArgs &a, int images, cudaStream_t s);
 cudaError_t launch_poc_cols(int n, const PassArgs &a, cudaStream_t s);
 
-// Streamed passes for 2048- and 4096-point lines (fft_stream.cu): whether
-// the pass applies to these arguments (contiguous complex images, 16-byte
-// aligned, the line count a multiple of the tile's; store mode ST_C2, or
-// ST_LOGMAG_MINMAX for a column pass over one image), and the launch, which
-// gives cudaErrorNotSupported when it does not apply.
+// The streamed column pass for 2048- and 4096-point columns (fft_stream.cu;
+// cols must be true): whether it applies to these arguments (contiguous
+// complex images, 16-byte aligned, the column count a multiple of the
+// tile's; store mode ST_C2, or ST_LOGMAG_MINMAX over one image), and the
+// launch, which gives cudaErrorNotSupported when it does not apply.
 bool stream_pass_applies(int n, bool cols, const PassArgs &a, int images, int st = ST_C2);
 cudaError_t launch_stream_pass(int n, bool cols, const PassArgs &a, int images, cudaStream_t s,
                                int st = ST_C2);

@@ -144,10 +144,11 @@ GLSFFT_API int glsfft_fft2d_tc(glsfft_context ctx, const void *src, void *dst, i
  * column pass each have schedules 0..6 per line length: 0 the default;
  * 1 half the elements per thread with the radix bound lowered to match;
  * 2 twice the elements per thread; 3 / 4 half / twice the lines or columns
- * per block; 5 = 1 and 3 together; 6 streamed: one persistent block per SM
- * that copies the next 128 KB tile in with the TMA while it transforms the
- * current one (lengths 2048 and 4096; bit-identical to schedule 0; calls
- * whose buffers are not 16-byte aligned run schedule 0).  All compute the
+ * per block; 5 = 1 and 3 together; 6 (column pass only) streamed: one
+ * persistent block per SM that copies the next 128 KB tile in with the TMA
+ * while it transforms the current one (lengths 2048 and 4096; bit-identical
+ * to schedule 0; calls whose buffers are not 16-byte aligned run schedule
+ * 0).  All compute the
  * same transform (rounding differs with the radix order, within the FP32
  * error bound).  Schedules 1..5 exist for lengths 64..4096 where the block
  * fits the SM.

@@ -113,5 +113,6 @@ def test_host_pipeline_and_schedule_calls_reject_bad_arguments(native):
     assert native.glsfft_schedule_available(1024, 7, 0) == 0
     assert native.glsfft_schedule_available(1024, 6, 0) == 0
     assert native.glsfft_schedule_available(4096, 6, 1) == 1
+    assert native.glsfft_schedule_available(4096, 6, 0) == 0
     assert native.glsfft_schedule_available(1000, 0, 0) == 0
     assert native.glsfft_schedule_available(16, 1, 1) == 0

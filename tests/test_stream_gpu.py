@@ -1,13 +1,15 @@
-"""Streamed long-line passes (pass schedule GLSFFT_SCHEDULE_STREAMED) on the GPU.
+"""The streamed column pass (pass schedule GLSFFT_SCHEDULE_STREAMED) on the GPU.
 
-The streamed row and column passes of 2048- and 4096-point lines compute
-with the plain kernels' arithmetic (same radix order, twiddles and rounding),
-so their output must be bit-identical to schedule 0 -- for every gls::fft
-flag combination (glsFft.h:43-47), batches of several images, in place
+The streamed column pass of 2048- and 4096-point columns computes with the
+plain kernels' arithmetic (same radix order, twiddles and rounding), so its
+output must be bit-identical to schedule 0 -- for every gls::fft flag
+combination (glsFft.h:43-47), batches of several images, in place
 (glsPhaseCorrelate.cpp:199 calls fft(C, C)) and through the single-pass
-entry points -- and arguments the streamed pass cannot take (a buffer that
-is only 8-byte aligned) must fall back to schedule 0.  No bounded wait may
-expire on the way.
+entry point -- and arguments it cannot take (a buffer that is only 8-byte
+aligned) must fall back to schedule 0.  No bounded wait may expire on the
+way.  The built-in default schedules (row schedule 2 for 2048/4096-point
+rows, the streamed pass for 4096-point columns) must equal schedule 0 bit
+for bit as well.
 """
 from __future__ import annotations
 
@@ -50,44 +52,39 @@ def _batch(rows, cols, count, seed):
 
 
 @pytest.mark.parametrize("rows,cols,count", [(4096, 4096, 1), (2048, 2048, 2), (2048, 1024, 3),
-                                             (1024, 2048, 2), (4096, 64, 2), (64, 4096, 1)])
+                                             (4096, 64, 2), (4096, 8, 1), (2048, 16, 2)])
 @pytest.mark.parametrize("flags", [0, INV | SCALE, SHIFT, INV | SCALE | SHIFT])
 def test_streamed_equals_schedule0(tctx, torch_cuda, rows, cols, count, flags):
-    if not (g.schedule_available(cols, STREAMED, False) or g.schedule_available(rows, STREAMED, True)):
-        pytest.skip("no streamed pass at this size")
     x = _batch(rows, cols, count, 1200 + rows + cols + flags)
     ref = _run(tctx, torch_cuda, x, rows, cols, flags, count, (0, 0))
-    rs = STREAMED if g.schedule_available(cols, STREAMED, False) else 0
-    cs = STREAMED if g.schedule_available(rows, STREAMED, True) else 0
-    got = _run(tctx, torch_cuda, x, rows, cols, flags, count, (rs, cs))
+    rs = 2 if g.schedule_available(cols, 2, False) else 0
+    got = _run(tctx, torch_cuda, x, rows, cols, flags, count, (rs, STREAMED))
     assert np.array_equal(ref.view(np.uint32), got.view(np.uint32))
-    got_ip = _run(tctx, torch_cuda, x, rows, cols, flags, count, (rs, cs), inplace=True)
+    got_ip = _run(tctx, torch_cuda, x, rows, cols, flags, count, (rs, STREAMED), inplace=True)
     assert np.array_equal(ref.view(np.uint32), got_ip.view(np.uint32))
     assert tctx.device_status() == 0
 
 
 def test_streamed_matches_fp64(tctx, torch_cuda, oracle):
     x = wl.complex_uniform(4096, 4096, 1299)
-    y = _run(tctx, torch_cuda, x, 4096, 4096, 0, 1, (STREAMED, STREAMED))
+    y = _run(tctx, torch_cuda, x, 4096, 4096, 0, 1, (0, STREAMED))
     ref64 = oracle.fft2d_f64(x)
     assert oracle.rel_l2(y, ref64) < 5e-7
-    back = _run(tctx, torch_cuda, y, 4096, 4096, INV | SCALE, 1, (STREAMED, STREAMED))
+    back = _run(tctx, torch_cuda, y, 4096, 4096, INV | SCALE, 1, (0, STREAMED))
     assert oracle.rel_l2(back, x) < 5e-7
 
 
-@pytest.mark.parametrize("along_rows", [True, False])
-def test_streamed_single_pass_entry_points(tctx, torch_cuda, along_rows):
+def test_streamed_single_pass_entry_point(tctx, torch_cuda):
     torch = torch_cuda
     s = stream_handle(torch)
     rows, cols, count = 4096, 2048, 2
     x = _batch(rows, cols, count, 1310)
     d = torch.from_numpy(x).cuda()
     outs = []
-    for sched in ((0, 0), (STREAMED, STREAMED)):
+    for sched in ((0, 0), (0, STREAMED)):
         tctx.set_fft_schedule(rows, cols, *sched)
         o = torch.empty_like(d)
-        fn = tctx.fft_rows if along_rows else tctx.fft_cols
-        fn(d.data_ptr(), o.data_ptr(), rows, cols, INV | SCALE | SHIFT, s, count)
+        tctx.fft_cols(d.data_ptr(), o.data_ptr(), rows, cols, INV | SCALE | SHIFT, s, count)
         torch.cuda.synchronize()
         outs.append(o.cpu().numpy())
     assert np.array_equal(outs[0].view(np.uint32), outs[1].view(np.uint32))
@@ -104,7 +101,7 @@ def test_streamed_falls_back_on_8_byte_alignment(tctx, torch_cuda):
     buf[1:] = torch.from_numpy(x.reshape(-1)).cuda()
     out = torch.zeros_like(buf)
     assert buf.data_ptr() % 16 == 0 and out.data_ptr() % 16 == 0
-    tctx.set_fft_schedule(n, n, STREAMED, STREAMED)
+    tctx.set_fft_schedule(n, n, 0, STREAMED)
     tctx.fft2d(buf.data_ptr() + 8, out.data_ptr() + 8, n, n, 0, s)
     torch.cuda.synchronize()
     got = out[1:].cpu().numpy().reshape(ref.shape)
@@ -114,9 +111,9 @@ def test_streamed_falls_back_on_8_byte_alignment(tctx, torch_cuda):
 
 def test_streamed_schedule_availability(native):
     for n in (2048, 4096):
-        assert g.schedule_available(n, STREAMED, False) and g.schedule_available(n, STREAMED, True)
+        assert g.schedule_available(n, STREAMED, True)       # column pass
+        assert not g.schedule_available(n, STREAMED, False)  # no row variant
     for n in (64, 1024):
-        assert not g.schedule_available(n, STREAMED, False)
         assert not g.schedule_available(n, STREAMED, True)
 
 
