@@ -390,7 +390,9 @@ int glsfft_device_status(glsfft_context ctx, int clear) {
     DeviceGuard g(ctx->device);
     if (!g.ok()) return GLSFFT_ERROR_CUDA;
     int v = 0;
-    cudaError_t e = cudaMemcpy(&v, ctx->d_status, sizeof(int), cudaMemcpyDeviceToHost);
+    // every stream of the device, blocking or not, has finished its work
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e == cudaSuccess) e = cudaMemcpy(&v, ctx->d_status, sizeof(int), cudaMemcpyDeviceToHost);
     if (e == cudaSuccess && clear && v) e = cudaMemset(ctx->d_status, 0, sizeof(int));
     if (e != cudaSuccess) return cuda_status(e);
     return v;
