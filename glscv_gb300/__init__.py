@@ -41,6 +41,7 @@ _SIGNATURES = {
     "glsfft_context_set_budget": (_ip, [_vp, _sz]),
     "glsfft_context_workspace": (_ip, [_vp, ctypes.POINTER(_sz)]),
     "glsfft_device_status": (_ip, [_vp, _ip]),
+    "glsfft_context_inject_stall": (_ip, [_vp, ctypes.c_longlong]),
     "glsfft_fft2d_c2c": (_ip, [_vp, _vp, _vp, _ip, _ip, _ip, _vp]),
     "glsfft_fft2d_r2c_promote": (_ip, [_vp, _vp, _vp, _ip, _ip, _ip, _vp]),
     "glsfft_fft_rows": (_ip, [_vp, _vp, _vp, _ip, _ip, _ip, _ip, _vp]),
@@ -207,6 +208,11 @@ class Context:
         """Sticky status of the context's device-side bounded waits (0 = none
         expired); synchronises with the device."""
         return int(lib().glsfft_device_status(self.handle, int(clear)))
+
+    def inject_stall(self, wait_limit_ns: int) -> None:
+        """Fault injection for tests: streamed passes leave their first tile
+        copies unissued and time out after wait_limit_ns (0: off)."""
+        check(lib().glsfft_context_inject_stall(self.handle, int(wait_limit_ns)), "inject_stall")
 
     def set_budget(self, nbytes: int) -> None:
         check(lib().glsfft_context_set_budget(self.handle, nbytes), "set_budget")

@@ -214,6 +214,7 @@ int glsfft::fft2d_launch(glsfft_context ctx, const void *src, void *dst, int row
                   (shift ? PF_SHIFT_COLS : 0u);
         a.tw = ctx->d_tw;
         a.err = ctx->d_status;
+        a.stall_ns = ctx->stall_ns;
         a.in_img_bytes = px * (real_in ? sizeof(float) : sizeof(float2));
         a.out_img_bytes = px * sizeof(float2);
         cudaError_t e = real_in ? launch_rows(cols, LD_R1, ST_C2, a, count, s)
@@ -231,6 +232,7 @@ int glsfft::fft2d_launch(glsfft_context ctx, const void *src, void *dst, int row
                   (shift ? PF_SHIFT_ROWS : 0u);
         a.tw = ctx->d_tw;
         a.err = ctx->d_status;
+        a.stall_ns = ctx->stall_ns;
         a.in_img_bytes = a.out_img_bytes = px * sizeof(float2);
         cudaError_t e = launch_cols_sched(rows, sc.col, a, count, s);
         if (e != cudaSuccess) return cuda_status(e);
@@ -385,6 +387,12 @@ int glsfft_context_destroy(glsfft_context ctx) {
     return GLSFFT_SUCCESS;
 }
 
+int glsfft_context_inject_stall(glsfft_context ctx, long long wait_limit_ns) {
+    if (!ctx || wait_limit_ns < 0) return GLSFFT_ERROR_INVALID_VALUE;
+    ctx->stall_ns = wait_limit_ns;
+    return GLSFFT_SUCCESS;
+}
+
 int glsfft_device_status(glsfft_context ctx, int clear) {
     if (!ctx) return GLSFFT_ERROR_INVALID_VALUE;
     DeviceGuard g(ctx->device);
@@ -484,6 +492,7 @@ static int one_pass(glsfft_context ctx, const void *src, void *dst, int count, i
               ((flags & GLSFFT_SHIFT) ? (along_rows ? PF_SHIFT_COLS : PF_SHIFT_ROWS) : 0u);
     a.tw = ctx->d_tw;
     a.err = ctx->d_status;
+        a.stall_ns = ctx->stall_ns;
     a.in_img_bytes = a.out_img_bytes = (size_t)rows * cols * sizeof(float2);
     const FftSchedule sc = schedule_for(ctx->sched, rows, cols);
     cudaError_t e = along_rows ? launch_rows_sched(n, sc.row, a, count, s)

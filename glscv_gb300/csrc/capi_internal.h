@@ -30,6 +30,7 @@ struct glsfft_context_s {
     std::map<long long, glsfft::FftSchedule> sched;
     HostPipe *host_pipe = nullptr;  // glsfft_fft2d_host's pipeline, built on first use
     int *d_status = nullptr;  // device status word of bounded waits (glsfft_device_status)
+    long long stall_ns = 0;   // glsfft_context_inject_stall (0: off)
 };
 
 namespace glsfft {

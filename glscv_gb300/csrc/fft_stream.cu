@@ -64,10 +64,12 @@ __host__ __device__ constexpr int stream_threads() {
 // batch as (rows * images) x cols 8-byte elements.
 template <int N>
 __device__ __forceinline__ void stream_issue(const CUtensorMap *tmap, const PassArgs &a, int tile,
-                                             int tpi, float2 *stage, unsigned long long *full) {
+                                             int tpi, float2 *stage, unsigned long long *full,
+                                             bool inject = false) {
     constexpr int L = stream_lines<N>();
     const int y0 = (tile / tpi) * a.rows, x = (tile % tpi) * L;
     mbar_arrive_tx(full, kStreamTileBytes);
+    if (inject) return;  // fault injection: the copy is never issued
 #pragma unroll
     for (int b = 0; b < N / 256; b++) tensor2d_g2s(stage + b * 256 * L, tmap, x, y0 + b * 256, full);
 }
@@ -102,15 +104,18 @@ __global__ void __launch_bounds__(stream_threads<N, E>(), 1)
     }
     __syncthreads();
     int tile = blockIdx.x;
-    if (tid == 0 && tile < total) stream_issue<N>(&tmap, a, tile, tpi, stage, full);
+    const bool inject = a.stall_ns > 0;
+    if (tid == 0 && tile < total) stream_issue<N>(&tmap, a, tile, tpi, stage, full, inject);
     unsigned parity = 0;
     MinMaxAny run;  // ST_LOGMAG_MINMAX only
+    const long long limit = inject ? a.stall_ns : kStreamWaitNs;
     for (; tile < total; tile += gridDim.x) {
-        const bool ok = mbar_wait(full, parity, kStreamWaitNs);
+        const bool ok = mbar_wait(full, parity, limit);
         if (__syncthreads_or(!ok)) {
             if (tid == 0) {
                 if (a.err) atomicExch(a.err, (int)GLSFFT_ERROR_TIMEOUT);
-                mbar_wait(full, parity, kStreamWaitNs);  // the copy in flight
+                // the copy in flight, if one was issued
+                if (!inject) mbar_wait(full, parity, kStreamWaitNs);
             }
             __syncthreads();
             return;

@@ -59,6 +59,10 @@ struct PassArgs {
     // device status word for bounded waits (the streamed passes record
     // GLSFFT_ERROR_TIMEOUT there), or null
     int *err;
+    // fault injection for tests (streamed passes): when > 0, each block
+    // leaves its first tile's copy unissued and waits this many nanoseconds
+    // for it, so the wait runs out
+    long long stall_ns;
 };
 
 // Launchers (fft_rows.cu, fft_cols.cu, poc.cu).  They return cudaSuccess or

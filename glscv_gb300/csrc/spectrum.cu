@@ -441,6 +441,7 @@ int glsfft_fft_display(glsfft_context ctx, const float *frame, const float *wind
         c.tw = ctx->d_tw;
         c.param = offset;
         c.err = ctx->d_status;
+        c.stall_ns = ctx->stall_ns;
         // 4096-point columns: the streamed pass (TMA-fed, one block per SM)
         e = rows == 4096 && stream_pass_applies(rows, true, c, 1, ST_LOGMAG_MINMAX)
                 ? launch_stream_pass(rows, true, c, 1, s, ST_LOGMAG_MINMAX)

@@ -86,6 +86,14 @@ GLSFFT_API int glsfft_context_workspace(glsfft_context ctx, size_t *bytes);
  * reference counterpart. */
 GLSFFT_API int glsfft_device_status(glsfft_context ctx, int clear);
 
+/* Host-side fault injection for tests: with wait_limit_ns > 0, every
+ * streamed pass launched on this context leaves each block's first tile copy
+ * unissued and bounds the wait for it by wait_limit_ns, so the wait runs
+ * out: the pass records GLSFFT_ERROR_TIMEOUT (glsfft_device_status) and
+ * returns with no copy in flight; the context stays usable.  0 turns the
+ * injection off. */
+GLSFFT_API int glsfft_context_inject_stall(glsfft_context ctx, long long wait_limit_ns);
+
 /*
  * 2-D complex FFT of a CV_32FC2 rows x cols device image:
  * gls::fft(src, dst, flag), glsCV/glsFft.h:55 / glsFft.cpp:675-708.

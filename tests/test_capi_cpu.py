@@ -82,6 +82,7 @@ def test_context_calls_reject_null(native):
     b = ctypes.c_size_t()
     assert native.glsfft_context_workspace(None, ctypes.byref(b)) == INVALID
     assert native.glsfft_device_status(None, 0) == INVALID
+    assert native.glsfft_context_inject_stall(None, 0) == INVALID
 
 
 def test_context_create_without_gpu_fails_cleanly(native):

@@ -24,6 +24,7 @@ pytestmark = pytest.mark.gpu
 
 INV, SCALE, SHIFT = 1, 2, 64
 STREAMED = 6
+TIMEOUT = 8  # GLSFFT_ERROR_TIMEOUT
 
 
 @pytest.fixture()
@@ -135,3 +136,22 @@ def test_builtin_default_schedules(tctx, torch_cuda):
     assert np.array_equal(ref.view(np.uint32), y.cpu().numpy().view(np.uint32))
     tctx.set_fft_schedule(4096, 4096, 2, STREAMED)                  # back to the default
     assert tctx.get_fft_schedule(4096, 4096) == (2, STREAMED)
+
+
+def test_streamed_stall_reports_timeout_and_context_recovers(tctx, torch_cuda):
+    # fault injection on the host side: each block's first tile copy is never
+    # issued, so its bounded wait (1 ms) runs out; the pass records
+    # GLSFFT_ERROR_TIMEOUT and returns with no copy in flight, and the same
+    # context then transforms correctly again
+    n = 4096
+    x = wl.complex_uniform(n, n, 1340)
+    ref = _run(tctx, torch_cuda, x, n, n, 0, 1, (0, 0))
+    assert tctx.device_status(clear=True) == 0
+    tctx.inject_stall(1_000_000)
+    _run(tctx, torch_cuda, x, n, n, 0, 1, (0, STREAMED))
+    assert tctx.device_status(clear=True) == TIMEOUT
+    assert tctx.device_status() == 0
+    tctx.inject_stall(0)
+    got = _run(tctx, torch_cuda, x, n, n, 0, 1, (0, STREAMED))
+    assert tctx.device_status() == 0
+    assert np.array_equal(ref.view(np.uint32), got.view(np.uint32))
