@@ -158,6 +158,53 @@ def traffic_per_launch(kernel: str):
 
 
 # -------------------------------------------------------------- CPU baseline
+def cpu_detail(reps: int = 3) -> dict:
+    """The CPU figures beside the baseline, each the median of `reps` timed
+    calls after one warm-up (wall clock): the radix-2 type1 Stockham on one
+    thread, the radix-4 Stockham driven one row / one column at a time (the
+    shader's algorithm, single thread), and phaseCorrelate restated on top
+    of the radix-2 Stockham on all host threads, all at 1024x1024.  The
+    reference's own compiled code is used where it was built (kind
+    "reference"), the restatement otherwise ("port")."""
+    import numpy as np
+    from glscv_gb300 import workloads as wl
+    from oracle import oracle as orc
+    orc.build()
+    ref = orc.ref_lib() is not None
+    x = wl.complex_uniform(ROWS, COLS, 5100)
+    a, b, _ = wl.shifted_pair(ROWS, COLS)
+    w = wl.hann_window(ROWS, COLS)
+    r2 = orc.ref_fft_r2t1_square if ref else orc.fft_r2t1_square
+    r4 = orc.ref_fft_r4_lines if ref else (lambda v: orc.fft2d(v, 0, 1))
+
+    def med(fn):
+        fn()
+        ts = []
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            fn()
+            ts.append(time.perf_counter() - t0)
+        return statistics.median(ts)
+
+    fwd_flops = flops_per_image() / 2
+    threads = os.cpu_count() or 1
+    orc.set_threads(1)
+    t_r2 = med(lambda: r2(x))
+    t_r4 = med(lambda: r4(x))
+    orc.set_threads(threads)
+    t_pc = med(lambda: orc.phase_correlate(a, b, w))
+    kind = "reference" if ref else "port"
+    return {
+        "size": f"{ROWS}x{COLS}", "reps": reps,
+        "r2t1_forward_1_thread": {"ms": round(t_r2 * 1e3, 2),
+                                  "gflops": round(fwd_flops / t_r2 / 1e9, 3), "kind": kind},
+        "r4_lines_forward_1_thread": {"ms": round(t_r4 * 1e3, 2),
+                                      "gflops": round(fwd_flops / t_r4 / 1e9, 3), "kind": kind},
+        "phase_correlate_ms": {"ms": round(t_pc * 1e3, 2), "threads": orc.num_threads(),
+                               "kind": "port (restatement over the radix-2 Stockham)"},
+    }
+
+
 def cpu_baseline(images: int, steps: int = 1, warmup: int = 0) -> dict:
     """The reference's CPU Stockham on all host threads over `images` images
     (forward + inverse each); returns value in GFLOP/s."""
@@ -794,6 +841,7 @@ def run_own(args) -> None:
 
     if rank == 0:
         cb = cpu_baseline(min(args.cpu_sample, B))
+        cpu_more = cpu_detail()
         serving = None if args.no_serving else serving_sweep(g, ctx, torch,
                                                              slots=args.serve_slots)
         precision = precision_form(ctx, torch, s)
@@ -821,6 +869,7 @@ def run_own(args) -> None:
                          "avg_launch_us": {k: round(v * 1e3, 3) for k, v in avg.items()},
                          "time_share": {k: round(v / sum(tot.values()), 4) for k, v in tot.items()}},
             "cpu_baseline": cb,
+            "cpu_detail": cpu_more,
             "e2e": e2e,
             "phase_correlate": pc,
             "serving": serving,
