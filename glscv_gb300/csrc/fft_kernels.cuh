@@ -126,27 +126,40 @@ __device__ __forceinline__ float2 load_elem(const void *img, const float *win, s
 // row-major order (glsPhaseCorrelate.cpp:60-137), response divided by
 // rows*cols (:224-225), shift = center - centroid (:228-230).
 // res[0..2] = dx, dy, response; res[3] = peak index as a double, res[4] = peak value.
-// Reads go to L2 (.cg): the surface was written by other blocks of this launch.
-__device__ __forceinline__ void poc_finish(const float *surface, int rows, int cols, int box,
-                                           unsigned long long k, double *res) {
-    int px = 0, py = 0;
-    double peak = -3.402823466e+38;
+struct PocBox {
+    int px, py, minr, maxr, minc, maxc;
+    double peak;
+};
+__device__ __forceinline__ PocBox poc_box(unsigned long long k, int rows, int cols, int box) {
+    PocBox b{0, 0, 0, 0, 0, 0, -3.402823466e+38};
     if (k != 0ull) {
         const unsigned idx = key_index(k);
-        px = (int)(idx % (unsigned)cols);
-        py = (int)(idx / (unsigned)cols);
-        peak = (double)key_value(k);
+        b.px = (int)(idx % (unsigned)cols);
+        b.py = (int)(idx / (unsigned)cols);
+        b.peak = (double)key_value(k);
     }
-    int minr = py - (box >> 1), maxr = py + (box >> 1);
-    int minc = px - (box >> 1), maxc = px + (box >> 1);
-    if (minr < 0) minr = 0;
-    if (minc < 0) minc = 0;
-    if (maxr > rows - 1) maxr = rows - 1;
-    if (maxc > cols - 1) maxc = cols - 1;
+    b.minr = b.py - (box >> 1);
+    b.maxr = b.py + (box >> 1);
+    b.minc = b.px - (box >> 1);
+    b.maxc = b.px + (box >> 1);
+    if (b.minr < 0) b.minr = 0;
+    if (b.minc < 0) b.minc = 0;
+    if (b.maxr > rows - 1) b.maxr = rows - 1;
+    if (b.maxc > cols - 1) b.maxc = cols - 1;
+    return b;
+}
+// The box values come from `vals` (row-major, width maxc - minc + 1) when
+// given, else straight from the surface through L2 (.cg: the surface was
+// written by other blocks of this launch).  Either way the sums run in the
+// reference's row-major order.
+__device__ __forceinline__ void poc_finish(const float *surface, int rows, int cols,
+                                           const PocBox &b, const float *vals, double *res) {
     double sx = 0.0, sy = 0.0, sum = 0.0;
-    for (int y = minr; y <= maxr; y++)
-        for (int x = minc; x <= maxc; x++) {
-            const double v = (double)__ldcg(surface + (size_t)y * cols + x);
+    const int w = b.maxc - b.minc + 1;
+    for (int y = b.minr; y <= b.maxr; y++)
+        for (int x = b.minc; x <= b.maxc; x++) {
+            const double v = vals ? (double)vals[(y - b.minr) * w + (x - b.minc)]
+                                  : (double)__ldcg(surface + (size_t)y * cols + x);
             sx += (double)x * v;
             sy += (double)y * v;
             sum += v;
@@ -156,9 +169,12 @@ __device__ __forceinline__ void poc_finish(const float *surface, int rows, int c
     res[0] = (double)cols / 2.0 - sx / sum;
     res[1] = (double)rows / 2.0 - sy / sum;
     res[2] = response;
-    res[3] = (double)(py * cols + px);
-    res[4] = peak;
+    res[3] = (double)(b.py * cols + b.px);
+    res[4] = b.peak;
 }
+// boxes up to this many values are read into shared memory by the whole
+// block at once (independent L2 reads in flight) before thread 0 sums them
+constexpr int kPocBoxCap = 1024;
 
 // ------------------------------------------------------------- row pass
 // Block: LINES rows x T threads.  blockIdx.y selects the image.  MB bounds
@@ -219,11 +235,21 @@ __global__ void __launch_bounds__(LINES *LineFft<N, E>::T)
                     s_last = prev == (unsigned long long)gridDim.x * gridDim.y - 1ull;
                 }
                 __syncthreads();
-                if (s_last && threadIdx.x == 0) {
+                if (s_last) {
+                    __shared__ float s_box[kPocBoxCap];
                     __threadfence();
-                    poc_finish(reinterpret_cast<const float *>(out), a.rows, N, a.box,
-                               __ldcg(a.key), a.result);
-                    __threadfence_system();  // result may be mapped host memory
+                    const float *surf = reinterpret_cast<const float *>(out);
+                    const PocBox b = poc_box(__ldcg(a.key), a.rows, N, a.box);
+                    const int w = b.maxc - b.minc + 1, n = w * (b.maxr - b.minr + 1);
+                    const bool staged = n <= kPocBoxCap;
+                    if (staged)
+                        for (int i = threadIdx.x; i < n; i += blockDim.x)
+                            s_box[i] = __ldcg(surf + (size_t)(b.minr + i / w) * N + b.minc + i % w);
+                    __syncthreads();
+                    if (threadIdx.x == 0) {
+                        poc_finish(surf, a.rows, N, b, staged ? s_box : nullptr, a.result);
+                        __threadfence_system();  // result may be mapped host memory
+                    }
                 }
             }
         }
