@@ -551,6 +551,43 @@ def spectrum_ops(ctx, torch, s, reps: int = 5, latency: bool = True) -> dict:
     return out
 
 
+def phase_correlate_device(ctx, torch, s, burst: int = 20) -> dict:
+    """phaseCorrelate device throughput per size: `burst` back-to-back
+    asynchronous calls (window included, result left on the device) between
+    two CUDA events, after 3 warm-up calls; algorithmic bytes 96 B/px (three
+    FFTs' worth, the reporting convention) against the measured HBM peak."""
+    from glscv_gb300 import workloads as wl
+    peak, peak_kind = measured_peaks()
+    stream = torch.cuda.current_stream()
+    res = torch.zeros(8, dtype=torch.float64, device="cuda")
+    out = {"peak_gbs": peak, "peak_kind": peak_kind, "burst": burst, "sizes": {}}
+    for n in (512, 1024, 2048, 4096):
+        a, b, _ = wl.shifted_pair(n, n)
+        w = wl.hann_window(n, n)
+        da, db, dw = (torch.from_numpy(v).cuda() for v in (a, b, w))
+
+        def call():
+            ctx.phase_correlate_async(da.data_ptr(), db.data_ptr(), dw.data_ptr(), n, n, 5,
+                                      res.data_ptr(), s)
+
+        for _ in range(3):
+            call()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(burst):
+            call()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / burst
+        gbs = 96.0 * n * n / (ms * 1e-3) / 1e9
+        out["sizes"][f"{n}x{n}"] = {"ms": round(ms, 4), "alg_gbs": round(gbs, 1),
+                                    "frac": round(gbs / peak, 4)}
+        del da, db, dw
+    return out
+
+
 def plain_single(ctx, torch, s) -> dict:
     """The plain drop-in path one image at a time (gls::fft per call): the
     256^2 forward + inverse(SCALE) case and single 1024^2 / 4096^2 images
@@ -848,6 +885,7 @@ def run_own(args) -> None:
         uneven = None if args.no_uneven else uneven_batch(g, ctx, torch, s, args.no_autotune)
         spectrum = spectrum_ops(ctx, torch, s)
         single = plain_single(ctx, torch, s)
+        pc_dev = phase_correlate_device(ctx, torch, s)
         line = {
             "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": round(ms, 4),
@@ -872,6 +910,7 @@ def run_own(args) -> None:
             "cpu_detail": cpu_more,
             "e2e": e2e,
             "phase_correlate": pc,
+            "phase_correlate_device": pc_dev,
             "serving": serving,
             "precision_form": precision,
             "uneven_batch": uneven,
