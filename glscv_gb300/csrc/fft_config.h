@@ -23,8 +23,11 @@ __host__ __device__ constexpr int cols_W(int n) {
 
 __host__ __device__ constexpr int poc_E(int n) { return cmin(n, 16); }
 __host__ __device__ constexpr int poc_T(int n) { return n / poc_E(n); }
+// 4 columns (32-byte row segments) at 256, 512 and 2048 points: a
+// phaseCorrelate image is one launch of a few hundred blocks at most, so
+// more, smaller blocks spread it over more SMs
 __host__ __device__ constexpr int poc_W(int n) {
-    return n == 4096 ? 2 : n == 2048 ? 4 : n == 1024 ? 8 : n == 512 ? 16 : cmax(16, cmin(64, 256 / poc_T(n)));
+    return n == 4096 ? 2 : n == 1024 ? 8 : n >= 256 ? 4 : cmax(16, cmin(64, 256 / poc_T(n)));
 }
 
 // shared-memory floats2 for `count` complex values with one pad per 16

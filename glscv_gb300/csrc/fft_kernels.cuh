@@ -246,10 +246,10 @@ __global__ void __launch_bounds__(LINES *LineFft<N, E>::T)
                         for (int i = threadIdx.x; i < n; i += blockDim.x)
                             s_box[i] = __ldcg(surf + (size_t)(b.minr + i / w) * N + b.minc + i % w);
                     __syncthreads();
-                    if (threadIdx.x == 0) {
+                    // (a result in mapped host memory needs no system fence:
+                    // the host reads it after synchronising with the kernel)
+                    if (threadIdx.x == 0)
                         poc_finish(surf, a.rows, N, b, staged ? s_box : nullptr, a.result);
-                        __threadfence_system();  // result may be mapped host memory
-                    }
                 }
             }
         }
@@ -342,18 +342,16 @@ __global__ void __launch_bounds__(W *LineFft<N, E>::T)
         a.key[1] = 0ull;
     }
 
+    // both lines' loads are issued up front, so the second line's latency
+    // overlaps the first line's transform
     float2 x[E], y[E];
 #pragma unroll
     for (int m = 0; m < E; m++) {
         const size_t i = (size_t)(t + m * T) * cols + col;
         y[m] = active ? __ldg(f2 + i) : make_float2(0.f, 0.f);
-    }
-    F::run(y, t, sm, a.tw);
-#pragma unroll
-    for (int m = 0; m < E; m++) {
-        const size_t i = (size_t)(t + m * T) * cols + col;
         x[m] = active ? __ldg(f1 + i) : make_float2(0.f, 0.f);
     }
+    F::run(y, t, sm, a.tw);
     __syncthreads();  // the exchange buffer is reused by the next line FFT
     if (!(a.flags & PF_F1_SPECTRUM)) {
         F::run(x, t, sm, a.tw);
