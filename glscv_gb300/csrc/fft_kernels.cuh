@@ -194,6 +194,15 @@ __global__ void __launch_bounds__(LINES *LineFft<N, E>::T)
     const void *in = image_in(a, blockIdx.y);
     void *out = image_out(a, blockIdx.y);
     const bool conj_in = a.flags & PF_CONJ_IN;
+    // a complex-output row pass given a key pointer zeroes the two keys for
+    // the kernel that follows it (the FFT display's column pass reduces its
+    // min / max there), saving a separate reset
+    if constexpr (ST == ST_C2) {
+        if (a.key && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) {
+            a.key[0] = 0ull;
+            a.key[1] = 0ull;
+        }
+    }
 
     float2 x[E];
 #pragma unroll

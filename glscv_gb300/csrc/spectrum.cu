@@ -414,9 +414,8 @@ int glsfft_fft_display(glsfft_context ctx, const float *frame, const float *wind
     if (st) return st;
     cudaStream_t s = (cudaStream_t)stream;
     float2 *spec = static_cast<float2 *>(ctx->ws);
-    cudaError_t e = cudaMemsetAsync(keys, 0, 2 * sizeof(unsigned long long), s);
-    if (e != cudaSuccess) return cuda_status(e);
-    // rows: window * frame promoted to complex, FFT of every row, half swap
+    // rows: window * frame promoted to complex, FFT of every row, half swap;
+    // the row kernel also zeroes the min / max keys
     PassArgs r{};
     r.in0 = frame;
     r.out0 = spec;
@@ -426,7 +425,8 @@ int glsfft_fft_display(glsfft_context ctx, const float *frame, const float *wind
     r.scale = 1.0f;
     r.flags = PF_SHIFT_COLS;
     r.tw = ctx->d_tw;
-    e = launch_rows(cols, window ? LD_R1W : LD_R1, ST_C2, r, 1, s);
+    r.key = keys;
+    cudaError_t e = launch_rows(cols, window ? LD_R1W : LD_R1, ST_C2, r, 1, s);
     if (e != cudaSuccess) return cuda_status(e);
     if (rows > 1) {
         // columns: FFT of every column, half swap, log(|X| + offset) and its min / max
