@@ -214,11 +214,7 @@ def cpu_baseline(images: int, steps: int = 1, warmup: int = 0) -> dict:
     orc.build()
     kind = "port"
     fwd = orc.fft_r2t1_square
-    if orc.ref_lib() is None and Path("/root/reference/UnitTest_glsCV/fft_stockhum.cpp").exists():
-        try:
-            orc.build_ref()
-        except Exception:
-            pass
+    # the reference's own Stockham where build() compiled it into oracle/_ref
     if orc.ref_lib() is not None:
         kind, fwd = "reference", orc.ref_fft_r2t1_square
     threads = os.cpu_count() or 1
