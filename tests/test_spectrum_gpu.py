@@ -102,10 +102,19 @@ def _mm_cases():
     zeros = np.array([[0.0, -0.0], [-0.0, 0.0]], np.float32)
     lit = np.full((3, 5), np.float32(3.4028233e38))            # beyond the shader's literal
     big = rng.standard_normal((4096, 4096)).astype(np.float32)
-    return [u, ties, nan, inf, zeros, lit, np.array([[2.5]], np.float32), big]
+    # large inputs: ties far apart (scanned by different blocks), and a size
+    # that is not a multiple of the blocks' stride
+    staged = np.zeros((2048, 2048), np.float32)
+    staged[3, 100] = staged[1500, 5] = staged[2047, 2047] = 7.0   # max: first is (100, 3)
+    staged[1000, 1000] = staged[10, 10] = -3.0                     # min: first is (10, 10)
+    staged[0, 0] = np.nan
+    tail = rng.uniform(-1, 1, (1500, 1500)).astype(np.float32)
+    tail[1499, 1000] = tail[1499, 1499] = 50.0                     # max: first is (1000, 1499)
+    tail[1499, 1200] = -50.0
+    return [u, ties, nan, inf, zeros, lit, np.array([[2.5]], np.float32), big, staged, tail]
 
 
-@pytest.mark.parametrize("case", range(8))
+@pytest.mark.parametrize("case", range(10))
 def test_min_max_loc_first_occurrence(ctx, torch_cuda, oracle, case):
     torch = torch_cuda
     x = _mm_cases()[case]
