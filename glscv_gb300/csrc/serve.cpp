@@ -2,16 +2,16 @@
 // and continuous batching.
 //
 // A server owns one device arena (its whole HBM budget, reserved once), a set
-// of slots (a CUDA stream, an event and a pinned result buffer each), and two
-// native threads:
+// of slots (a CUDA stream, an event and a mapped pinned result buffer each),
+// and native threads of two kinds:
 //   * dispatchers (kDispatchers threads) admit queued requests in arrival
-//     order as soon as a slot
-//     is free and the request's workspace fits in the arena (looking a few
-//     requests past a head that does not fit yet), and launches the request's
-//     whole pipeline on the slot's stream: host->device copy of the frame,
-//     windowed row FFT, phase-only column kernel against the resident
-//     reference spectrum (so 2 FFTs per request instead of 3), inverse row FFT
-//     with the argmax, FP64 centroid, device->host copy of the result;
+//     order as soon as a slot is free and the request's workspace fits in the
+//     arena (looking a few requests past a head that does not fit yet), and
+//     launch the request's whole pipeline on the slot's stream: host->device
+//     copy of the frame, windowed row FFT, phase-only column kernel against
+//     the resident reference spectrum (so 2 FFTs per request instead of 3),
+//     inverse row FFT with the argmax, whose last block writes the FP64
+//     centroid straight into the slot's result buffer;
 //   * the completion poller watches the slots' events (queried without the
 //     lock), stamps completion times, returns workspaces to the arena and
 //     wakes the dispatchers.
