@@ -44,6 +44,9 @@ def parse():
     p.add_argument("--impl", choices=["own", "reference"], default="own")
     p.add_argument("--images", type=int, default=64, help="images per step per GPU")
     p.add_argument("--cpu-sample", type=int, default=2, help="images per CPU-baseline step")
+    p.add_argument("--cpu-seconds", type=float, default=10.0,
+                   help="CPU time the default run's CPU baseline samples (steps of --cpu-sample "
+                        "images, median)")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-serving", action="store_true", help="skip the serving sweep")
     p.add_argument("--profile-only", action="store_true",
@@ -205,9 +208,11 @@ def cpu_detail(reps: int = 3) -> dict:
     }
 
 
-def cpu_baseline(images: int, steps: int = 1, warmup: int = 0) -> dict:
+def cpu_baseline(images: int, steps: int = 1, warmup: int = 0, min_seconds: float = 0.0) -> dict:
     """The reference's CPU Stockham on all host threads over `images` images
-    (forward + inverse each); returns value in GFLOP/s."""
+    (forward + inverse each) per step; at least `steps` steps and, with
+    min_seconds, as many more as fit in that much CPU time (a bounded sample
+    of the workload); the median step gives the value in GFLOP/s."""
     import numpy as np
     from glscv_gb300 import workloads as wl
     from oracle import oracle as orc
@@ -231,7 +236,8 @@ def cpu_baseline(images: int, steps: int = 1, warmup: int = 0) -> dict:
     for _ in range(warmup):
         one_step()
     t = []
-    for _ in range(steps):
+    start = time.perf_counter()
+    while len(t) < steps or time.perf_counter() - start < min_seconds:
         t0 = time.perf_counter()
         one_step()
         t.append(time.perf_counter() - t0)
@@ -239,8 +245,8 @@ def cpu_baseline(images: int, steps: int = 1, warmup: int = 0) -> dict:
     value = images * flops_per_image() / sec / 1e9
     return {"value": round(value, 3), "unit": UNIT, "cores": orc.num_threads(), "kind": kind,
             "sample": f"{images} x {ROWS}x{COLS} images forward+inverse per step "
-                      f"(fft_dit_Stockham_radix2_type1), median of {steps} step(s), "
-                      f"{sec * 1e3:.1f} ms per step"}
+                      f"(fft_dit_Stockham_radix2_type1), median of {len(t)} step(s) over "
+                      f"{time.perf_counter() - start:.1f} s, {sec * 1e3:.1f} ms per step"}
 
 
 def run_reference(args) -> None:
@@ -873,7 +879,7 @@ def run_own(args) -> None:
               "note": "1024x1024 CV_32FC1 pair + Hann window, one call at a time, host wall clock"}
 
     if rank == 0:
-        cb = cpu_baseline(min(args.cpu_sample, B))
+        cb = cpu_baseline(min(args.cpu_sample, B), warmup=1, min_seconds=args.cpu_seconds)
         cpu_more = cpu_detail()
         serving = None if args.no_serving else serving_sweep(g, ctx, torch,
                                                              slots=args.serve_slots)
