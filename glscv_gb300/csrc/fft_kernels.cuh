@@ -148,26 +148,35 @@ __device__ __forceinline__ PocBox poc_box(unsigned long long k, int rows, int co
     if (b.maxc > cols - 1) b.maxc = cols - 1;
     return b;
 }
-// The box values come from `vals` (row-major, width maxc - minc + 1) when
-// given, else straight from the surface through L2 (.cg: the surface was
-// written by other blocks of this launch).  Either way the sums run in the
-// reference's row-major order.
-__device__ __forceinline__ void poc_finish(const float *surface, int rows, int cols,
-                                           const PocBox &b, const float *vals, double *res) {
-    double sx = 0.0, sy = 0.0, sum = 0.0;
+// One of the centroid's three FP64 sums over the box in the reference's
+// row-major order: which = 0: sum of x*v, 1: sum of y*v, 2: sum of v.  The
+// products and sums are rounded separately (no fused multiply-add), as the
+// reference's CPU code computes them.  The box values come from `vals`
+// (row-major, width maxc - minc + 1) when given, else straight from the
+// surface through L2 (.cg: the surface was written by other blocks of this
+// launch).
+__device__ __forceinline__ double poc_sum(const float *surface, int cols, const PocBox &b,
+                                          const float *vals, int which) {
+    double acc = 0.0;
     const int w = b.maxc - b.minc + 1;
     for (int y = b.minr; y <= b.maxr; y++)
         for (int x = b.minc; x <= b.maxc; x++) {
             const double v = vals ? (double)vals[(y - b.minr) * w + (x - b.minc)]
                                   : (double)__ldcg(surface + (size_t)y * cols + x);
-            sx += (double)x * v;
-            sy += (double)y * v;
-            sum += v;
+            acc = which == 2 ? __dadd_rn(acc, v)
+                             : __dadd_rn(acc, __dmul_rn((double)(which == 0 ? x : y), v));
         }
+    return acc;
+}
+// The result from the three sums: response = sum / (rows*cols)
+// (:224-225), then sum + DBL_EPSILON divides (:128), shift = center -
+// centroid (:228-230).
+__device__ __forceinline__ void poc_result(int rows, int cols, const PocBox &b, double sx,
+                                           double sy, double sum, double *res) {
     const double response = sum / ((double)rows * (double)cols);
-    sum += 2.220446049250313e-16;  // DBL_EPSILON, glsPhaseCorrelate.cpp:128
-    res[0] = (double)cols / 2.0 - sx / sum;
-    res[1] = (double)rows / 2.0 - sy / sum;
+    sum = __dadd_rn(sum, 2.220446049250313e-16);  // DBL_EPSILON, glsPhaseCorrelate.cpp:128
+    res[0] = __dsub_rn((double)cols / 2.0, sx / sum);
+    res[1] = __dsub_rn((double)rows / 2.0, sy / sum);
     res[2] = response;
     res[3] = (double)(b.py * cols + b.px);
     res[4] = b.peak;
@@ -255,10 +264,18 @@ __global__ void __launch_bounds__(LINES *LineFft<N, E>::T)
                         for (int i = threadIdx.x; i < n; i += blockDim.x)
                             s_box[i] = __ldcg(surf + (size_t)(b.minr + i / w) * N + b.minc + i % w);
                     __syncthreads();
-                    // (a result in mapped host memory needs no system fence:
-                    // the host reads it after synchronising with the kernel)
+                    // the three FP64 sums on lane 0 of three warps (separate
+                    // SM partitions), then thread 0 forms the result (a result
+                    // in mapped host memory needs no system fence: the host
+                    // reads it after synchronising with the kernel)
+                    __shared__ double s_sum[3];
+                    const int warp = threadIdx.x >> 5, warps = (blockDim.x + 31) >> 5;
+                    if ((threadIdx.x & 31) == 0)
+                        for (int which = warp; which < 3; which += warps)
+                            s_sum[which] = poc_sum(surf, N, b, staged ? s_box : nullptr, which);
+                    __syncthreads();
                     if (threadIdx.x == 0)
-                        poc_finish(surf, a.rows, N, b, staged ? s_box : nullptr, a.result);
+                        poc_result(a.rows, N, b, s_sum[0], s_sum[1], s_sum[2], a.result);
                 }
             }
         }

@@ -72,6 +72,11 @@ def lib():
             _f32p, _f32p, _f32p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
             ctypes.c_int, _dp, _dp, _dp, _f32p, _ip]
         l.oracle_max_loc.argtypes = [_f32p, ctypes.c_int, ctypes.c_int, _ip, _ip, _f32p]
+        l.oracle_centroid.argtypes = [_f32p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                      ctypes.POINTER(ctypes.c_double),
+                                      ctypes.POINTER(ctypes.c_double),
+                                      ctypes.POINTER(ctypes.c_double), _ip]
+        l.oracle_centroid.restype = None
         l.oracle_mul_spectrums.argtypes = [_f32p, _f32p, _f32p, ctypes.c_size_t, ctypes.c_int]
         l.oracle_mul_spectrums_poc.argtypes = [_f32p, _f32p, _f32p, ctypes.c_size_t]
         l.oracle_mag_spectrums.argtypes = [_f32p, _f32p, ctypes.c_size_t, ctypes.c_int,
@@ -160,6 +165,16 @@ def max_loc(c: np.ndarray):
     lib().oracle_max_loc(_fp(c), c.shape[0], c.shape[1], ctypes.byref(px), ctypes.byref(py),
                          ctypes.byref(mv))
     return (px.value, py.value), mv.value
+
+
+def centroid(surface: np.ndarray, box: int = 5):
+    """The tail of gls::phaseCorrelate on a given surface: ((dx, dy), response, peak)."""
+    c = np.ascontiguousarray(surface, dtype=np.float32)
+    dx, dy, resp = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+    peak = (ctypes.c_int * 2)()
+    lib().oracle_centroid(_fp(c), c.shape[0], c.shape[1], int(box), ctypes.byref(dx),
+                          ctypes.byref(dy), ctypes.byref(resp), ctypes.cast(peak, _ip))
+    return (dx.value, dy.value), resp.value, (peak[0], peak[1])
 
 
 def phase_correlate(a: np.ndarray, b: np.ndarray, window: np.ndarray | None = None,

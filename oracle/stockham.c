@@ -388,6 +388,25 @@ int oracle_phase_correlate(const float *a, const float *b, const float *window, 
     return 0;
 }
 
+/*
+ * The tail of gls::phaseCorrelate on a given correlation surface
+ * (glsPhaseCorrelate.cpp:205-231): first-max location, clamped-box FP64
+ * weighted centroid, response = sum / (rows*cols), shift = center - centroid.
+ * Lets a test check the GPU's centroid arithmetic on the GPU's own surface.
+ */
+void oracle_centroid(const float *surface, int rows, int cols, int box, double *dx, double *dy,
+                     double *response, int *peak_xy) {
+    int px, py;
+    oracle_max_loc(surface, rows, cols, &px, &py, NULL);
+    double cx, cy, s;
+    weighted_centroid(surface, rows, cols, px, py, box, &cx, &cy, &s);
+    *response = s / ((double)rows * (double)cols);
+    *dx = (double)cols / 2.0 - cx;
+    *dy = (double)rows / 2.0 - cy;
+    peak_xy[0] = px;
+    peak_xy[1] = py;
+}
+
 /* Element-wise helpers for the spectrum-op family
  * (glsBasicOperation.cpp:153-212, :320-351). */
 void oracle_mul_spectrums(const float *a, const float *b, float *out, size_t n, int conj) {

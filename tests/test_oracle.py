@@ -164,3 +164,13 @@ def test_normalize_and_spectrum_restatements(oracle):
     assert np.allclose(np.abs(p), 1, atol=1e-6)
     z = oracle.mul_spectrums_phase_only(np.zeros_like(a), b)
     assert np.isnan(z.view(np.float32)).all()  # 0/0, no epsilon (glsBasicOperation.cpp:202-205)
+
+
+def test_centroid_matches_phase_correlate_tail(oracle):
+    # the centroid entry point is the tail of the oracle's own phaseCorrelate
+    from glscv_gb300 import workloads as wl
+    a, b = wl.random_pair(128, 128, seed=77, shift=(9.25, -3.5))
+    win = wl.hann_window(128, 128)
+    (dx, dy), resp, peak, surf = oracle.phase_correlate(a, b, win, box=5, want_surface=True)
+    (cx, cy), cresp, cpeak = oracle.centroid(surf, 5)
+    assert (dx, dy, resp, tuple(peak)) == (cx, cy, cresp, cpeak)

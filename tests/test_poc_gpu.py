@@ -117,3 +117,23 @@ def test_budget_error(native, torch_cuda):
             c.phase_correlate(d.data_ptr(), d.data_ptr(), None, 64, 64)
         assert e.value.status == 7
         assert c.workspace_bytes() == 0
+
+
+@pytest.mark.parametrize("shape,box,shift", [((256, 256), 5, (7.3, -4.6)),
+                                             ((1024, 1024), 5, (-100.0, 37.0)),
+                                             ((512, 256), 3, (11.5, 3.25)),
+                                             ((64, 64), 7, (2.2, -1.7)),
+                                             ((128, 128), 5, (64.0, 63.0)),      # box clamped
+                                             ((2048, 2048), 5, (5.5, -5.5))])
+def test_centroid_bit_exact_on_gpu_surface(ctx, torch_cuda, oracle, shape, box, shift):
+    # on the GPU's own correlation surface, the first-max location and the
+    # FP64 weighted centroid / response (separately rounded products and sums,
+    # glsPhaseCorrelate.cpp:60-137, :205-231) equal the reference's
+    # arithmetic bit for bit
+    rows, cols = shape
+    a, b = wl.random_pair(rows, cols, seed=rows + 3 * cols + box, shift=shift)
+    win = wl.hann_window(rows, cols)
+    (gx, gy), gresp, gsurf = gpu_phase_correlate(ctx, torch_cuda, a, b, win, box=box,
+                                                 want_surface=True)
+    (ox, oy), oresp, _ = oracle.centroid(gsurf, box)
+    assert (gx, gy, gresp) == (ox, oy, oresp)
