@@ -42,6 +42,11 @@ _SIGNATURES = {
     "glsfft_context_workspace": (_ip, [_vp, ctypes.POINTER(_sz)]),
     "glsfft_device_status": (_ip, [_vp, _ip]),
     "glsfft_context_inject_stall": (_ip, [_vp, ctypes.c_longlong]),
+    "glsfft_fft2d_reference": (_ip, [_vp, _vp, _vp, _ip, _ip, _ip, _ip, _ip, _vp]),
+    "glsfft_phase_correlate_reference": (_ip, [_vp, _vp, _vp, _vp, _ip, _ip, _ip, _ip,
+                                               ctypes.POINTER(ctypes.c_double),
+                                               ctypes.POINTER(ctypes.c_double),
+                                               ctypes.POINTER(ctypes.c_double), _vp]),
     "glsfft_fft2d_c2c": (_ip, [_vp, _vp, _vp, _ip, _ip, _ip, _vp]),
     "glsfft_fft2d_r2c_promote": (_ip, [_vp, _vp, _vp, _ip, _ip, _ip, _vp]),
     "glsfft_fft_rows": (_ip, [_vp, _vp, _vp, _ip, _ip, _ip, _ip, _vp]),
@@ -164,6 +169,22 @@ class Context:
                       flags: int = 0, stream: int = 0) -> None:
         check(lib().glsfft_fft2d_batched(self.handle, src, dst, count, rows, cols, flags, stream),
               "fft2d_batched")
+
+    def fft2d_reference(self, src: int, dst: int, rows: int, cols: int, flags: int = 0,
+                        algo: int = 0, stream: int = 0, count: int = 1) -> None:
+        """Reference-arithmetic gls::fft (bit-identical to the reference's CPU
+        Stockham: algo 0 radix-2 type1, 1 radix-4 lines)."""
+        check(lib().glsfft_fft2d_reference(self.handle, src, dst, count, rows, cols, flags, algo,
+                                           stream), "fft2d_reference")
+
+    def phase_correlate_reference(self, src1: int, src2: int, window: int | None, rows: int,
+                                  cols: int, box: int = 5, algo: int = 0, stream: int = 0):
+        dx, dy, resp = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        check(lib().glsfft_phase_correlate_reference(self.handle, src1, src2, window or None,
+                                                     rows, cols, box, algo, ctypes.byref(dx),
+                                                     ctypes.byref(dy), ctypes.byref(resp),
+                                                     stream), "phase_correlate_reference")
+        return (dx.value, dy.value), resp.value
 
     def fft2d_tc(self, src: int, dst: int, count: int, rows: int, cols: int, flags: int = 0,
                  stream: int = 0) -> None:

@@ -382,6 +382,7 @@ int glsfft_context_destroy(glsfft_context ctx) {
     if (ctx->d_tw) cudaFree(ctx->d_tw);
     if (ctx->h_result) cudaFreeHost(ctx->h_result);
     if (ctx->d_status) cudaFree(ctx->d_status);
+    for (auto &t : ctx->exact_tw) cudaFree(t.second);
     tc_tables_destroy(&ctx->tc);
     delete ctx;
     return GLSFFT_SUCCESS;

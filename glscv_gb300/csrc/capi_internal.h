@@ -31,6 +31,8 @@ struct glsfft_context_s {
     HostPipe *host_pipe = nullptr;  // glsfft_fft2d_host's pipeline, built on first use
     int *d_status = nullptr;  // device status word of bounded waits (glsfft_device_status)
     long long stall_ns = 0;   // glsfft_context_inject_stall (0: off)
+    // the reference-arithmetic mode's twiddle tables, per line length
+    std::map<int, float2 *> exact_tw;
 };
 
 namespace glsfft {
@@ -55,6 +57,10 @@ int check_poc_args(glsfft_context ctx, const float *src1, const float *src2,
                    const float *window, int rows, int cols, int box);
 int fft2d_launch(glsfft_context ctx, const void *src, void *dst, int rows, int cols, int flags,
                  bool real_in, cudaStream_t s, int count = 1);
+// The reference-arithmetic transform (fft_exact.cu): `count` images src ->
+// dst through tmp (count * rows * cols complex, apart from src and dst).
+int fft2d_exact_launch(glsfft_context ctx, const void *src, void *dst, void *tmp, int count,
+                       int rows, int cols, int flags, int algo, cudaStream_t s);
 
 constexpr int kMaxBatch = 65535;  // grid y extent
 int poc_launch(const float2 *tw, const float *src1, const float *src2, const float *window,

@@ -136,6 +136,31 @@ GLSFFT_API int glsfft_fft_cols(glsfft_context ctx, const void *src, void *dst, i
                                int rows, int cols, int flags, void *stream);
 
 /*
+ * Reference-arithmetic mode (verification; no reference counterpart as an
+ * entry point): gls::fft over `count` back-to-back images computed with the
+ * reference's own FP32 line arithmetic -- algo 0: the radix-2 DIT type1
+ * Stockham of UnitTest_glsCV/fft_stockhum.cpp:436-538, algo 1: the radix-4
+ * DIT Stockham of :866-1031 (the GLSL shader's algorithm, glsFft.cpp:
+ * 203-343) -- with the reference's twiddle table ((float) angle, cosf/sinf)
+ * and every product and sum rounded separately, so the result is
+ * bit-identical to the reference's CPU routine with gls::fft's flag
+ * semantics.  Several times slower than glsfft_fft2d_c2c; uses the context
+ * workspace.
+ */
+GLSFFT_API int glsfft_fft2d_reference(glsfft_context ctx, const void *src, void *dst, int count,
+                                      int rows, int cols, int flags, int algo, void *stream);
+/* gls::phaseCorrelate (glsPhaseCorrelate.cpp:142-236) on the reference-
+ * arithmetic FFT: window product, forward FFTs, phase-only spectrum without
+ * epsilon (0/0 -> NaN, as the reference), unscaled inverse with the quadrant
+ * shift, real part, first-max location, FP64 centroid; synchronous.  Every
+ * step rounds as the reference's CPU code, so dx, dy and response are
+ * bit-identical to it on the same inputs. */
+GLSFFT_API int glsfft_phase_correlate_reference(glsfft_context ctx, const float *src1,
+                                                const float *src2, const float *window, int rows,
+                                                int cols, int box, int algo, double *dx,
+                                                double *dy, double *response, void *stream);
+
+/*
  * Precision form of the batched 2-D FFT (no reference counterpart): each
  * 1024- or 4096-point line is a four-step FFT (32 x 32 or 64 x 64) whose two
  * DFT stages run as complex matrix products on the tensor cores with FP16

@@ -83,6 +83,9 @@ def test_context_calls_reject_null(native):
     assert native.glsfft_context_workspace(None, ctypes.byref(b)) == INVALID
     assert native.glsfft_device_status(None, 0) == INVALID
     assert native.glsfft_context_inject_stall(None, 0) == INVALID
+    assert native.glsfft_fft2d_reference(None, None, None, 1, 16, 16, 0, 0, None) == INVALID
+    assert native.glsfft_phase_correlate_reference(None, None, None, None, 16, 16, 5, 0,
+                                                   None, None, None, None) == INVALID
 
 
 def test_context_create_without_gpu_fails_cleanly(native):
