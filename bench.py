@@ -590,6 +590,39 @@ def phase_correlate_device(ctx, torch, s, burst: int = 20) -> dict:
     return out
 
 
+def reference_mode(ctx, torch, s) -> dict:
+    """The reference-arithmetic mode (bit-identical to the reference's CPU
+    Stockham): forward transforms of one 1024^2 and one 4096^2 image per
+    algorithm, CUDA events, median of 5 after 2."""
+    import numpy as np
+    from glscv_gb300 import workloads as wl
+    stream = torch.cuda.current_stream()
+    out = {}
+    for n in (1024, 4096):
+        d = torch.from_numpy(wl.complex_uniform(n, n, 7)).cuda()
+        y = torch.empty_like(d)
+        for algo, name in ((0, "radix2_type1"), (1, "radix4_lines")):
+            def call():
+                ctx.fft2d_reference(d.data_ptr(), y.data_ptr(), n, n, 0, algo, s)
+            for _ in range(2):
+                call()
+            ts = []
+            for _ in range(5):
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                call()
+                e1.record(stream)
+                torch.cuda.synchronize()
+                ts.append(e0.elapsed_time(e1))
+            ms = sorted(ts)[2]
+            out[f"{n}x{n}_{name}"] = {
+                "forward_ms": round(ms, 4),
+                "gflops": round(5.0 * n * n * np.log2(n * n) / (ms * 1e-3) / 1e9, 1)}
+    out["note"] = "bit-identical to the reference's CPU routines (tests/test_reference_mode_gpu.py)"
+    return out
+
+
 def plain_single(ctx, torch, s) -> dict:
     """The plain drop-in path one image at a time (gls::fft per call): the
     256^2 forward + inverse(SCALE) case and single 1024^2 / 4096^2 images
@@ -888,6 +921,7 @@ def run_own(args) -> None:
         spectrum = spectrum_ops(ctx, torch, s)
         single = plain_single(ctx, torch, s)
         pc_dev = phase_correlate_device(ctx, torch, s)
+        ref_mode = reference_mode(ctx, torch, s)
         line = {
             "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": round(ms, 4),
@@ -913,6 +947,7 @@ def run_own(args) -> None:
             "e2e": e2e,
             "phase_correlate": pc,
             "phase_correlate_device": pc_dev,
+            "reference_arithmetic": ref_mode,
             "serving": serving,
             "precision_form": precision,
             "uneven_batch": uneven,
