@@ -181,6 +181,40 @@ Point2d phaseCorrelate(const GlsMat &src1, const GlsMat &src2, GlsMat &window, d
     return phaseCorrelate(src1, src2, window, response, 5);
 }
 
+// ----------------------------------------------- reference-arithmetic mode
+void fftReference(const GlsMat &src, GlsMat &dst, int flag, int algo) {
+    assert_that(!src.empty(), "gls::fftReference: empty src");
+    assert_that(src.type() == CV_32FC2, "gls::fftReference: src must be CV_32FC2");
+    GlsMat out = out_for(dst, src.size(), CV_32FC2);
+    check(glsfft_fft2d_reference(context(), src.devptr(), out.devptr(), 1, src.rows, src.cols,
+                                 flag, algo, nullptr),
+          "gls::fftReference");
+    dst = out;
+}
+
+Point2d phaseCorrelateReference(const GlsMat &src1, const GlsMat &src2, GlsMat &window,
+                                double *response, int algo) {
+    assert_that(!src1.empty() && !src2.empty(), "gls::phaseCorrelateReference: empty input");
+    assert_that(src1.type() == src2.type() && src1.type() == CV_32FC1,
+                "gls::phaseCorrelateReference: inputs must be CV_32FC1");
+    if (src1.size() != src2.size())
+        throw Exception(GLSFFT_ERROR_SHAPE, "gls::phaseCorrelateReference");
+    if (!window.empty()) {
+        assert_that(window.type() == CV_32FC1, "gls::phaseCorrelateReference: window must be CV_32FC1");
+        if (window.size() != src1.size())
+            throw Exception(GLSFFT_ERROR_SHAPE, "gls::phaseCorrelateReference");
+    }
+    double dx = 0, dy = 0, res = 0;
+    check(glsfft_phase_correlate_reference(
+              context(), static_cast<const float *>(src1.devptr()),
+              static_cast<const float *>(src2.devptr()),
+              window.empty() ? nullptr : static_cast<const float *>(window.devptr()), src1.rows,
+              src1.cols, 5, algo, &dx, &dy, &res, nullptr),
+          "gls::phaseCorrelateReference");
+    if (response) *response = res;
+    return Point2d(dx, dy);
+}
+
 // ------------------------------------------------------ spectrum operations
 namespace {
 void check_spectrum(const GlsMat &m, const char *where) {

@@ -153,6 +153,16 @@ GLS_EXPORT Point2d phaseCorrelate(const GlsMat &src1, const GlsMat &src2, GlsMat
 GLS_EXPORT Point2d phaseCorrelate(const GlsMat &src1, const GlsMat &src2, GlsMat &window,
                                   double *response, int box);
 
+// Extensions (not in the reference): the same operations computed with the
+// reference's own CPU Stockham arithmetic -- algo 0: the radix-2 type1
+// routine, 1: the radix-4 routine per line (the shader's algorithm) -- so the
+// results are bit-identical to it (glsfft_fft2d_reference,
+// glsfft_phase_correlate_reference).  fftReference takes CV_32FC2 only.
+GLS_EXPORT void fftReference(const GlsMat &src, GlsMat &dst, int flag = 0, int algo = 0);
+GLS_EXPORT Point2d phaseCorrelateReference(const GlsMat &src1, const GlsMat &src2,
+                                           GlsMat &window, double *response = 0,
+                                           int algo = 0);
+
 // glsCV/glsBasicOperation.h:78-88: CV_32FC2 spectra; dst is (re)allocated
 // like getDstMat does (CV_32FC2 for the products, CV_32FC1 for magnitudes).
 GLS_EXPORT void mulSpectrums(const GlsMat &src0, const GlsMat &src1, GlsMat &dst,

@@ -144,6 +144,43 @@ static void test_phase_correlate() {
     EXPECT(std::fabs(s2.x - dx) < 0.05 && std::fabs(s2.y - dy) < 0.05, "phaseCorrelate, no window");
     Mat a2 = ga;
     EXPECT(a2.ptr<float>()[17] == a.ptr<float>()[17], "inputs left unchanged");
+    // the reference-arithmetic extension finds the same shift
+    for (int algo = 0; algo < 2; algo++) {
+        double rresp = 0;
+        gls::Point2d r = gls::phaseCorrelateReference(ga, gb, gw, &rresp, algo);
+        EXPECT(std::fabs(r.x - s.x) < 1e-3 && std::fabs(r.y - s.y) < 1e-3,
+               "phaseCorrelateReference agrees with phaseCorrelate");
+        EXPECT(std::fabs(rresp - resp) < 1e-4, "phaseCorrelateReference response");
+    }
+}
+
+static void test_fft_reference() {
+    const int rows = 32, cols = 64;
+    Mat a(rows, cols, gls::CV_32FC2);
+    std::mt19937 rng(11);
+    std::uniform_real_distribution<float> u(-1.f, 1.f);
+    for (size_t i = 0; i < 2 * a.total(); i++) a.ptr<float>()[i] = u(rng);
+    GlsMat ga(a), fast, exact;
+    gls::fft(ga, fast, gls::GLS_FFT_SHIFT);
+    for (int algo = 0; algo < 2; algo++) {
+        gls::fftReference(ga, exact, gls::GLS_FFT_SHIFT, algo);
+        Mat f = fast, e = exact;
+        double num = 0, den = 0;
+        for (size_t i = 0; i < 2 * a.total(); i++) {
+            const double d = (double)f.ptr<float>()[i] - e.ptr<float>()[i];
+            num += d * d;
+            den += (double)e.ptr<float>()[i] * e.ptr<float>()[i];
+        }
+        EXPECT(std::sqrt(num / den) < 1e-6, "fftReference agrees with fft within FP32 rounding");
+    }
+    // in place, as gls::fft allows
+    GlsMat c = ga.clone();
+    gls::fftReference(c, c, 0, 0);
+    gls::fftReference(ga, exact, 0, 0);
+    Mat cm = c, em = exact;
+    bool same = true;
+    for (size_t i = 0; i < 2 * a.total(); i++) same &= cm.ptr<float>()[i] == em.ptr<float>()[i];
+    EXPECT(same, "fftReference in place equals out of place");
 }
 
 static void test_errors() {
@@ -251,6 +288,7 @@ int main() {
     gls::glsCvInit(0);
     test_fft();
     test_phase_correlate();
+    test_fft_reference();
     test_errors();
     test_spectrum_ops();
     gls::glsCvTerminate();
