@@ -248,8 +248,15 @@ __global__ void __launch_bounds__(LINES *LineFft<N, E>::T)
                 // key update are released before its count) computes the centroid
                 __shared__ int s_last;
                 if (threadIdx.x == 0) {
-                    __threadfence();
-                    const unsigned long long prev = atomicAdd(a.key + 1, 1ull);
+                    // one acquire-release add instead of a full fence and a
+                    // relaxed add: it releases this block's surface writes
+                    // (ordered before it by the barrier in the key commit)
+                    // and, in the last block, acquires every other block's
+                    unsigned long long prev;
+                    asm volatile("atom.acq_rel.gpu.global.add.u64 %0, [%1], 1;"
+                                 : "=l"(prev)
+                                 : "l"(a.key + 1)
+                                 : "memory");
                     s_last = prev == (unsigned long long)gridDim.x * gridDim.y - 1ull;
                 }
                 __syncthreads();
