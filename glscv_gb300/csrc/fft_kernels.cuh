@@ -345,6 +345,17 @@ __global__ void __launch_bounds__(W *LineFft<N, E>::T)
     }
 }
 
+// conj(P) for the phaseCorrelate column kernels: P = F1 conj(F2) / |F1 conj(F2)|
+// (glsBasicOperation.cpp:195-206, every product and sum rounded separately,
+// as the shader formula restated in spectrum_device.cuh), conjugated because
+// the inverse is taken as conj(FFT(conj P)); |t| = 0 gives 0, not 0/0.
+__device__ __forceinline__ float2 poc_conj_phase(float2 f1, float2 f2) {
+    const float2 t = spec_mul<true>(f1, f2);
+    const float mag = sqrtf(__fadd_rn(__fmul_rn(t.x, t.x), __fmul_rn(t.y, t.y)));
+    return mag > 0.f ? make_float2(__fdiv_rn(t.x, mag), -__fdiv_rn(t.y, mag))
+                     : make_float2(0.f, 0.f);
+}
+
 // --------------------------------------------- fused phaseCorrelate columns
 // in0 = row-pass output of src1 (or, with PF_F1_SPECTRUM, its resident full
 // 2-D spectrum), in1 = row-pass output of src2.  Each block finishes the
@@ -391,14 +402,7 @@ __global__ void __launch_bounds__(W *LineFft<N, E>::T)
         __syncthreads();
     }
 #pragma unroll
-    for (int m = 0; m < E; m++) {
-        const float2 s0 = x[m], s1 = y[m];
-        const float tr = s0.x * s1.x + s0.y * s1.y;
-        const float ti = -s0.x * s1.y + s0.y * s1.x;
-        const float mag = sqrtf(tr * tr + ti * ti);
-        // conj(P): the inverse is taken as conj(FFT(conj P))
-        x[m] = mag > 0.f ? make_float2(tr / mag, -(ti / mag)) : make_float2(0.f, 0.f);
-    }
+    for (int m = 0; m < E; m++) x[m] = poc_conj_phase(x[m], y[m]);
     F::run(x, t, sm, a.tw);
     float2 *out = reinterpret_cast<float2 *>(a.out0);
 #pragma unroll
