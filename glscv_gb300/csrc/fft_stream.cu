@@ -178,119 +178,7 @@ cudaError_t stream_launch(const PassArgs &a, int images, cudaStream_t s) {
     return cudaGetLastError();
 }
 
-// ------------------------------------------- streamed phaseCorrelate columns
-// The fused phaseCorrelate column kernel (poc_cols_kernel) on the same
-// pipeline for 2048-point columns: a tile is 4 columns of both spectra
-// (f2 then f1, 64 KB each, 8 boxes of 4 x 256 through one tensor map each),
-// so the next tile's copies fly while the block transforms, multiplies and
-// inverse-transforms the current one.  Same line engine, phase-only formula
-// and output as poc_cols_kernel: bit-identical results.
-constexpr int kPocN = 2048, kPocE = 16, kPocL = 4;
-constexpr int kPocT = kPocN / kPocE;
-constexpr unsigned kPocHalfBytes = kPocL * kPocN * sizeof(float2);  // 64 KB per spectrum
-constexpr size_t kPocXchgBytes = ((size_t)col_split_floats(kPocL * kPocN) * sizeof(float) + 15) & ~size_t(15);
-constexpr size_t kPocSmem = 128 + 2 * (size_t)kPocHalfBytes + kPocXchgBytes + 16;
-
-__device__ __forceinline__ void poc_issue(const CUtensorMap *m1, const CUtensorMap *m2, int tile,
-                                          float2 *stage, unsigned long long *full) {
-    mbar_arrive_tx(full, 2 * kPocHalfBytes);
-#pragma unroll
-    for (int b = 0; b < kPocN / 256; b++) {
-        tensor2d_g2s(stage + b * 256 * kPocL, m2, tile * kPocL, b * 256, full);
-        tensor2d_g2s(stage + kPocL * kPocN + b * 256 * kPocL, m1, tile * kPocL, b * 256, full);
-    }
-}
-
-__global__ void __launch_bounds__(kPocL * kPocT, 1)
-    fft_stream_poc(const __grid_constant__ CUtensorMap m1, const __grid_constant__ CUtensorMap m2,
-                   const PassArgs a) {
-    using F = LineFft<kPocN, kPocE, SyncBlock, 4>;
-    extern __shared__ unsigned char stream_raw[];
-    unsigned char *base = stream_raw + ((128u - (smem_u32(stream_raw) & 127u)) & 127u);
-    float2 *stage = reinterpret_cast<float2 *>(base);
-    float *xch = reinterpret_cast<float *>(base + 2 * kPocHalfBytes);
-    unsigned long long *full =
-        reinterpret_cast<unsigned long long *>(base + 2 * kPocHalfBytes + kPocXchgBytes);
-    const int tid = threadIdx.x, l = tid % kPocL, t = tid / kPocL;
-    const int total = a.cols / kPocL;
-    // the argmax key and the block counter of the inverse row pass that follows
-    if (a.key && blockIdx.x == 0 && tid == 0) {
-        a.key[0] = 0ull;
-        a.key[1] = 0ull;
-    }
-    if (tid == 0) {
-        mbar_init(full, 1);
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    }
-    __syncthreads();
-    int tile = blockIdx.x;
-    if (tid == 0 && tile < total) poc_issue(&m1, &m2, tile, stage, full);
-    unsigned parity = 0;
-    const bool f1_spectrum = a.flags & PF_F1_SPECTRUM;
-    for (; tile < total; tile += gridDim.x) {
-        const bool ok = mbar_wait(full, parity, kStreamWaitNs);
-        if (__syncthreads_or(!ok)) {
-            if (tid == 0) {
-                if (a.err) atomicExch(a.err, (int)GLSFFT_ERROR_TIMEOUT);
-                mbar_wait(full, parity, kStreamWaitNs);  // the copies in flight
-            }
-            __syncthreads();
-            return;
-        }
-        parity ^= 1u;
-        float2 x[kPocE], y[kPocE];
-#pragma unroll
-        for (int m = 0; m < kPocE; m++) {
-            y[m] = stage[(t + m * kPocT) * kPocL + l];
-            x[m] = stage[kPocL * kPocN + (t + m * kPocT) * kPocL + l];
-        }
-        __syncthreads();  // the stage is free for the next tile's copies
-        const int next = tile + gridDim.x;
-        if (tid == 0 && next < total) poc_issue(&m1, &m2, next, stage, full);
-        ColSmF<kPocL> sm{xch, l};
-        F::run(y, t, sm, a.tw);
-        __syncthreads();  // the exchange buffer is reused by the next line FFT
-        if (!f1_spectrum) {
-            F::run(x, t, sm, a.tw);
-            __syncthreads();
-        }
-#pragma unroll
-        for (int m = 0; m < kPocE; m++) x[m] = poc_conj_phase(x[m], y[m]);
-        F::run(x, t, sm, a.tw);
-        float2 *out = reinterpret_cast<float2 *>(a.out0);
-        const int col = tile * kPocL + l;
-#pragma unroll
-        for (int m = 0; m < kPocE; m++) out[(size_t)(t + m * kPocT) * a.cols + col] = x[m];
-    }
-}
-
 }  // namespace
-
-bool stream_poc_applies(int n, const PassArgs &a) {
-    if (n != kPocN || a.rows != n || a.cols < kPocL || a.cols % kPocL) return false;
-    if (!a.in0 || !a.in1 || !a.out0) return false;
-    const uintptr_t p0 = reinterpret_cast<uintptr_t>(a.in0), p1 = reinterpret_cast<uintptr_t>(a.in1),
-                    po = reinterpret_cast<uintptr_t>(a.out0);
-    return (p0 % 16) == 0 && (p1 % 16) == 0 && (po % 16) == 0;
-}
-
-cudaError_t launch_stream_poc(int n, const PassArgs &a, cudaStream_t s) {
-    if (!stream_poc_applies(n, a)) return cudaErrorNotSupported;
-    CUtensorMap m1{}, m2{};
-    if (make_tmap_2d(&m1, a.in0, a.cols, a.rows, kPocL, 256) != GLSFFT_SUCCESS ||
-        make_tmap_2d(&m2, a.in1, a.cols, a.rows, kPocL, 256) != GLSFFT_SUCCESS)
-        return cudaErrorNotSupported;
-    cudaError_t e = smem_opt_in(reinterpret_cast<const void *>(fft_stream_poc), kPocSmem);
-    if (e != cudaSuccess) return e;
-    int dev = 0, sms = 0;
-    e = cudaGetDevice(&dev);
-    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (e != cudaSuccess) return e;
-    if (sms <= 0) return cudaErrorNotSupported;
-    const int total = a.cols / kPocL;
-    fft_stream_poc<<<total < sms ? total : sms, kPocL * kPocT, kPocSmem, s>>>(m1, m2, a);
-    return cudaGetLastError();
-}
 
 bool stream_pass_applies(int n, bool cols, const PassArgs &a, int images, int st) {
     if (!cols || (n != 2048 && n != 4096)) return false;

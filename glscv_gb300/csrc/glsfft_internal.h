@@ -80,12 +80,6 @@ bool stream_pass_applies(int n, bool cols, const PassArgs &a, int images, int st
 cudaError_t launch_stream_pass(int n, bool cols, const PassArgs &a, int images, cudaStream_t s,
                                int st = ST_C2);
 
-// The streamed phaseCorrelate column pass for 2048-point columns
-// (fft_stream.cu): applies to 16-byte aligned spectra with a column count
-// that is a multiple of 4; the launch gives cudaErrorNotSupported otherwise.
-bool stream_poc_applies(int n, const PassArgs &a);
-cudaError_t launch_stream_poc(int n, const PassArgs &a, cudaStream_t s);
-
 // A 2-D tensor map over a row-major array of 8-byte elements (width x
 // height, rows `width` elements apart) with a box_w x box_h box, for TMA
 // copies (batch.cpp).  GLSFFT_SUCCESS or an error status.

@@ -2,7 +2,6 @@
 // into the inverse row pass, fft_kernels.cuh).
 #include "fft_config.h"
 #include "fft_kernels.cuh"
-#include "glsfft_internal.h"
 
 namespace glsfft {
 
@@ -22,8 +21,6 @@ static cudaError_t poc_t(const PassArgs &a, cudaStream_t s) {
 }
 
 cudaError_t launch_poc_cols(int n, const PassArgs &a, cudaStream_t s) {
-    // 2048-point columns: the streamed pass (TMA-fed, one block per SM)
-    if (n == 2048 && stream_poc_applies(n, a)) return launch_stream_poc(n, a, s);
     switch (n) {
     case 1: return poc_t<1>(a, s);
     case 2: return poc_t<2>(a, s);
