@@ -65,6 +65,9 @@ def parse():
                    help="run only the serving sweep and print its JSON")
     p.add_argument("--profile-spectrum", action="store_true",
                    help="run each spectrum operation once on 4096x4096 and exit (for ncu)")
+    p.add_argument("--profile-pc", type=int, default=0, metavar="N",
+                   help="run phaseCorrelate (Hann window) on one NxN pair three times and exit "
+                        "(for ncu)")
     p.add_argument("--profile-fft", type=int, default=0, metavar="N",
                    help="run gls::fft forward on one NxN image three times with the size's "
                         "default pass schedules and exit (for ncu)")
@@ -762,6 +765,20 @@ def run_own(args) -> None:
 
     if args.serving_only:
         print(json.dumps(serving_sweep(g, ctx, torch, slots=args.serve_slots)), flush=True)
+        ctx.close()
+        return
+
+    if args.profile_pc:
+        # the synchronous phaseCorrelate call: three calls, for ncu
+        n = args.profile_pc
+        a, b, _ = wl.shifted_pair(n, n)
+        w = wl.hann_window(n, n)
+        da, db, dw = (torch.from_numpy(v).cuda() for v in (a, b, w))
+        shift = None
+        for _ in range(3):
+            shift = ctx.phase_correlate(da.data_ptr(), db.data_ptr(), dw.data_ptr(), n, n, 5, s)
+        print(json.dumps({"profile_pc": n, "shift": list(shift[0]), "response": shift[1]}),
+              flush=True)
         ctx.close()
         return
 
