@@ -4,12 +4,22 @@
 
 namespace glsfft {
 
+// The real-input and argmax row passes (phaseCorrelate, the FFT display,
+// promoted CV_32FC1 input) take row schedule 2's shape on 2048- and
+// 4096-point rows -- 32 values per thread, as the complex pass does by
+// default there -- with the same radix order, so the same results.
+template <int N, int LD, int ST>
+constexpr PassShape rows_fixed_shape() {
+    return (N >= 2048 && !(LD == LD_C2 && ST == ST_C2)) ? row_shape(N, 2) : row_shape(N, 0);
+}
+
 template <int N, int LD, int ST>
 static cudaError_t rows_t(const PassArgs &a, int images, cudaStream_t s) {
-    constexpr int E = rows_E(N), LINES = rows_LINES(N), T = rows_T(N);
+    constexpr PassShape sh = rows_fixed_shape<N, LD, ST>();
+    constexpr int E = sh.E, LINES = sh.G, T = N / E;
     constexpr int threads = LINES * T;
     constexpr size_t smem = num_passes(N) > 1 ? sizeof(float2) * (size_t)LINES * padded_count(N) : 0;
-    auto kern = fft_rows_kernel<N, E, LINES, LD, ST>;
+    auto kern = fft_rows_kernel<N, E, LINES, LD, ST, sh.MB>;
     if constexpr (smem > 48 * 1024) {
         const cudaError_t e = smem_opt_in(reinterpret_cast<const void *>(kern), smem);
         if (e != cudaSuccess) return e;
