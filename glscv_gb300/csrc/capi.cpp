@@ -248,7 +248,9 @@ int glsfft::poc_launch(const float2 *tw, const float *src1, const float *src2,
                        cudaStream_t s) {
     // three launches: rows of both images; fused POC columns (which also
     // zero the argmax key and block counter); inverse rows with the argmax
-    // and, in the last block, the centroid
+    // and, in the last block, the centroid.  All three use programmatic
+    // dependent launch, so each grid is resident and waiting when its
+    // predecessor (the previous call's last pass, for the first) ends.
     PassArgs a{};
     a.in0 = src1;
     a.in1 = src2;
@@ -259,6 +261,7 @@ int glsfft::poc_launch(const float2 *tw, const float *src1, const float *src2,
     a.cols = cols;
     a.scale = 1.0f;
     a.tw = tw;
+    a.pdl = 1;
     cudaError_t e = launch_rows(cols, window ? LD_R1W : LD_R1, ST_C2, a, 2, s);
     if (e != cudaSuccess) return cuda_status(e);
 
@@ -271,6 +274,7 @@ int glsfft::poc_launch(const float2 *tw, const float *src1, const float *src2,
     b.scale = 1.0f;
     b.key = key;
     b.tw = tw;
+    b.pdl = 1;
     e = launch_poc_cols(rows, b, s);
     if (e != cudaSuccess) return cuda_status(e);
 
@@ -285,6 +289,7 @@ int glsfft::poc_launch(const float2 *tw, const float *src1, const float *src2,
     c.tw = tw;
     c.result = d_result;
     c.box = box;
+    c.pdl = 1;
     e = launch_rows(cols, LD_C2, ST_RE_ARGMAX, c, 1, s);
     return cuda_status(e);
 }

@@ -108,6 +108,38 @@ __device__ __forceinline__ void *image_out(const PassArgs &a, unsigned z) {
     return static_cast<char *>(a.out0) + (size_t)z * a.out_img_bytes;
 }
 
+// Programmatic dependent launch.  A pass launched with PassArgs::pdl can be
+// made resident while its stream predecessor is still running; it waits here,
+// before its first global access, until that grid has completed and its
+// memory is visible, then lets its own successor launch.  Both instructions
+// return at once in a grid launched without the attribute.
+__device__ __forceinline__ void pdl_enter() {
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+// Launch one pass kernel, with the programmatic-serialisation attribute when
+// a.pdl is set (the kernel must begin with pdl_enter()).
+template <typename Kern>
+inline cudaError_t launch_pass(Kern kern, dim3 grid, unsigned threads, size_t smem,
+                               cudaStream_t s, const PassArgs &a) {
+    if (!a.pdl) {
+        kern<<<grid, threads, smem, s>>>(a);
+        return cudaGetLastError();
+    }
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = dim3(threads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kern, a);
+}
+
 // ------------------------------------------------------------ load / store
 template <int LD>
 __device__ __forceinline__ float2 load_elem(const void *img, const float *win, size_t idx) {
@@ -196,6 +228,7 @@ __global__ void __launch_bounds__(LINES *LineFft<N, E>::T)
     extern __shared__ float4 smem_raw[];
     float2 *smem = reinterpret_cast<float2 *>(smem_raw);
     __shared__ unsigned long long red[(LINES * T + 31) / 32];
+    pdl_enter();
 
     const int l = threadIdx.x / T, t = threadIdx.x % T;
     const int row = blockIdx.x * LINES + l;
@@ -380,6 +413,7 @@ __global__ void __launch_bounds__(W *LineFft<N, E>::T)
     const float2 *f1 = reinterpret_cast<const float2 *>(a.in0);
     const float2 *f2 = reinterpret_cast<const float2 *>(a.in1);
     ColSm<W> sm{smem, c};
+    pdl_enter();
     // the argmax key and the block counter of the inverse row pass that follows
     if (a.key && blockIdx.x == 0 && threadIdx.x == 0) {
         a.key[0] = 0ull;

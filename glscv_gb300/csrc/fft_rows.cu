@@ -25,8 +25,7 @@ static cudaError_t rows_t(const PassArgs &a, int images, cudaStream_t s) {
         if (e != cudaSuccess) return e;
     }
     dim3 grid((a.rows + LINES - 1) / LINES, images);
-    kern<<<grid, threads, smem, s>>>(a);
-    return cudaGetLastError();
+    return launch_pass(kern, grid, threads, smem, s, a);
 }
 
 template <int LD, int ST>

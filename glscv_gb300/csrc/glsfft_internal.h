@@ -63,6 +63,9 @@ struct PassArgs {
     // leaves its first tile's copy unissued and waits this many nanoseconds
     // for it, so the wait runs out
     long long stall_ns;
+    // launch with programmatic dependent launch (row and POC column passes
+    // only): the grid may become resident before its stream predecessor ends
+    int pdl;
 };
 
 // Launchers (fft_rows.cu, fft_cols.cu, poc.cu).  They return cudaSuccess or

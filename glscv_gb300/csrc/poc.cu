@@ -16,8 +16,7 @@ static cudaError_t poc_t(const PassArgs &a, cudaStream_t s) {
         if (e != cudaSuccess) return e;
     }
     dim3 grid((a.cols + W - 1) / W, 1);
-    kern<<<grid, threads, smem, s>>>(a);
-    return cudaGetLastError();
+    return launch_pass(kern, grid, threads, smem, s, a);
 }
 
 cudaError_t launch_poc_cols(int n, const PassArgs &a, cudaStream_t s) {

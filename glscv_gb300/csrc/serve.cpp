@@ -143,6 +143,7 @@ int launch_request(glsfft_server srv, const Reference &ref, const Request &rq, S
     b.flags = PF_F1_SPECTRUM;
     b.key = key;
     b.tw = srv->ctx->d_tw;
+    b.pdl = 1;  // resident while the row pass drains
     e = launch_poc_cols(rows, b, s);
     if (e != cudaSuccess) return cuda_status(e);
     PassArgs c{};
@@ -156,6 +157,7 @@ int launch_request(glsfft_server srv, const Reference &ref, const Request &rq, S
     c.tw = srv->ctx->d_tw;
     c.result = slot.h_result_dev;
     c.box = rq.box;
+    c.pdl = 1;
     e = launch_rows(cols, LD_C2, ST_RE_ARGMAX, c, 1, s);
     if (e == cudaSuccess) e = cudaEventRecord(slot.done, s);
     return cuda_status(e);
