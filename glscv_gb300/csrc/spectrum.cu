@@ -180,13 +180,16 @@ __global__ void __launch_bounds__(kThreads) minmax_kernel(const float *__restric
         const float4 *x4 = reinterpret_cast<const float4 *>(x);
         // eight independent 16-byte loads in flight before the compares (a
         // read-only stream needs more bytes in flight per thread than a copy;
-        // the visiting order per thread stays increasing)
+        // the visiting order per thread stays increasing).  The last batch is
+        // predicated, its missing slots NaN, which never compares, so the
+        // ragged end costs one round trip rather than one per load.
         constexpr int kBatch = 8;
-        size_t i = tid;
-        for (; i + (kBatch - 1) * stride < nv; i += kBatch * stride) {
+        const float4 none = make_float4(__int_as_float(0x7fffffff), __int_as_float(0x7fffffff),
+                                        __int_as_float(0x7fffffff), __int_as_float(0x7fffffff));
+        for (size_t i = tid; i < nv; i += kBatch * stride) {
             float4 v[kBatch];
 #pragma unroll
-            for (int k = 0; k < kBatch; k++) v[k] = x4[i + k * stride];
+            for (int k = 0; k < kBatch; k++) v[k] = i + k * stride < nv ? x4[i + k * stride] : none;
 #pragma unroll
             for (int k = 0; k < kBatch; k++) {
                 const unsigned b = (unsigned)(4 * (i + k * stride));
@@ -195,13 +198,6 @@ __global__ void __launch_bounds__(kThreads) minmax_kernel(const float *__restric
                 run.add(v[k].z, b + 2);
                 run.add(v[k].w, b + 3);
             }
-        }
-        for (; i < nv; i += stride) {
-            const float4 v = x4[i];
-            run.add(v.x, (unsigned)(4 * i));
-            run.add(v.y, (unsigned)(4 * i + 1));
-            run.add(v.z, (unsigned)(4 * i + 2));
-            run.add(v.w, (unsigned)(4 * i + 3));
         }
         done = nv * 4;
     }
@@ -227,15 +223,16 @@ __global__ void __launch_bounds__(kThreads) normalize_kernel(const float *x, flo
             return make_float4(__fadd_rn(c, __fmul_rn(scl, v.x)), __fadd_rn(c, __fmul_rn(scl, v.y)),
                                __fadd_rn(c, __fmul_rn(scl, v.z)), __fadd_rn(c, __fmul_rn(scl, v.w)));
         };
-        size_t i = tid;
-        for (; i + 3 * stride < nv; i += 4 * stride) {  // four loads in flight
+        // four loads in flight; the last batch predicated (one round trip)
+        for (size_t i = tid; i < nv; i += 4 * stride) {
             float4 v[4];
 #pragma unroll
-            for (int k = 0; k < 4; k++) v[k] = x4[i + k * stride];
+            for (int k = 0; k < 4; k++)
+                v[k] = i + k * stride < nv ? x4[i + k * stride] : make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
-            for (int k = 0; k < 4; k++) d4[i + k * stride] = step(v[k]);
+            for (int k = 0; k < 4; k++)
+                if (i + k * stride < nv) d4[i + k * stride] = step(v[k]);
         }
-        for (; i < nv; i += stride) d4[i] = step(x4[i]);
         done = nv * 4;
     }
     for (size_t i = done + tid; i < n; i += stride) d[i] = __fadd_rn(c, __fmul_rn(scl, x[i]));
