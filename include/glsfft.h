@@ -383,8 +383,10 @@ GLSFFT_API int glsfft_batch_get_schedule(glsfft_batch plan, int *schedule4);
  * is timed, `reps` graph launches
  * each (median, CUDA events on `stream`), on a shadow plan of the same
  * shapes, flags, alignments and aliasing over scratch buffers, so the
- * plan's own images are never read or written.  The fastest is applied to
- * the plan unless the default schedule is within 1% of it.  With cache_path
+ * plan's own images are never read or written.  The six fastest and the
+ * default are then timed again in three interleaved rounds (each keeps the
+ * median of its three medians); the fastest of those is applied to the plan
+ * unless the default schedule is within 1% of it.  With cache_path
  * set, the choice is looked up in / appended to that plan cache file
  * (keyed by device, driver, library version, the plan's size histograms and
  * flags); a hit is applied without timing.
