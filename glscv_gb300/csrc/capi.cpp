@@ -174,6 +174,10 @@ cudaError_t glsfft::smem_opt_in(const void *kern, size_t bytes) {
 }
 
 int glsfft::ensure_workspace(glsfft_context ctx, size_t bytes) {
+    // every user of the workspace overwrites (or frees) the last
+    // phaseCorrelate's surface; the phaseCorrelate calls record theirs after
+    ctx->surface = nullptr;
+    ctx->surface_count = 0;
     if (bytes <= ctx->ws_bytes) return GLSFFT_SUCCESS;
     if (ctx->budget && bytes > ctx->budget) return GLSFFT_ERROR_BUDGET;
     if (ctx->ws) {

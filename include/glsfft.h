@@ -449,7 +449,10 @@ GLSFFT_API int glsfft_phase_correlate_async(glsfft_context ctx, const float *src
  * phaseCorrelate on this context (the plane the reference downloads for its
  * centroid, glsPhaseCorrelate.cpp:219) into the device buffer `dst` of
  * `count` floats (count must equal rows*cols of that call).  Asynchronous
- * on `stream`.  For tests and debugging.
+ * on `stream`.  For tests and debugging.  The surface lives in the context
+ * workspace: a later call that uses the workspace (the reference-arithmetic
+ * FFT, minMaxLoc / normalize / FFT display with context keys) discards it,
+ * and this call then returns GLSFFT_ERROR_SHAPE.
  */
 GLSFFT_API int glsfft_phase_correlate_surface(glsfft_context ctx, float *dst, size_t count,
                                               void *stream);

@@ -164,3 +164,18 @@ def test_back_to_back_async_calls_match_synchronous(ctx, torch_cuda, n):
     for i, (da, db) in enumerate(pairs):
         (dx, dy), resp = ctx.phase_correlate(da.data_ptr(), db.data_ptr(), w.data_ptr(), n, n, 5, s)
         assert (got[i, 0], got[i, 1], got[i, 2]) == (dx, dy, resp)
+
+
+def test_surface_discarded_by_a_later_workspace_user(ctx, torch_cuda, oracle):
+    # the surface lives in the context workspace: a minMaxLoc that takes its
+    # keys from the workspace overwrites it, and the copy is then refused
+    import glscv_gb300 as g
+    torch = torch_cuda
+    a, b = wl.random_pair(64, 64, seed=4100, shift=(3.0, -2.0))
+    (_, _), _, surf = gpu_phase_correlate(ctx, torch, a, b, None, box=5, want_surface=True)
+    assert surf.shape == (64, 64)
+    f = torch.rand(64, 64, device="cuda")
+    ctx.min_max_loc(f.data_ptr(), 64, 64)
+    d_surf = torch.empty((64, 64), dtype=torch.float32, device="cuda")
+    with pytest.raises(g.GlsError):
+        ctx.copy_surface(d_surf.data_ptr(), 64 * 64)
