@@ -268,7 +268,10 @@ def run_reference(args) -> None:
         "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
         "note": "reference GPU path is OpenGL 3.3 fragment shaders: unavailable on this box; "
-                "the reference's own CPU Stockham is timed instead",
+                "the reference's CPU Stockham is timed instead ("
+                + ("its own code, compiled from its sources" if cb.get("kind") == "reference"
+                   else "the oracle's restatement, bit-identical to the reference's compiled "
+                        "routine") + ")",
     }
     print(json.dumps(line), flush=True)
 
