@@ -179,3 +179,31 @@ def test_surface_discarded_by_a_later_workspace_user(ctx, torch_cuda, oracle):
     d_surf = torch.empty((64, 64), dtype=torch.float32, device="cuda")
     with pytest.raises(g.GlsError):
         ctx.copy_surface(d_surf.data_ptr(), 64 * 64)
+
+
+def test_async_call_captured_in_cuda_graph(ctx, torch_cuda):
+    # the three chained launches captured into a CUDA graph (programmatic
+    # dependencies become graph edges) and replayed give the synchronous result
+    torch = torch_cuda
+    n = 512
+    a, b = wl.random_pair(n, n, seed=4200, shift=(12.4, -7.7))
+    da = torch.from_numpy(np.ascontiguousarray(a, np.float32)).cuda()
+    db = torch.from_numpy(np.ascontiguousarray(b, np.float32)).cuda()
+    w = torch.from_numpy(wl.hann_window(n, n)).cuda()
+    res = torch.zeros(8, dtype=torch.float64, device="cuda")
+    side = torch.cuda.Stream()
+    # first call outside the capture: workspace and kernel attributes are set up
+    ctx.phase_correlate_async(da.data_ptr(), db.data_ptr(), w.data_ptr(), n, n, 5,
+                              res.data_ptr(), side.cuda_stream)
+    torch.cuda.synchronize()
+    res.zero_()
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph, stream=side):
+        ctx.phase_correlate_async(da.data_ptr(), db.data_ptr(), w.data_ptr(), n, n, 5,
+                                  res.data_ptr(), side.cuda_stream)
+    for _ in range(3):
+        graph.replay()
+    torch.cuda.synchronize()
+    got = res.cpu().numpy()
+    (dx, dy), resp = ctx.phase_correlate(da.data_ptr(), db.data_ptr(), w.data_ptr(), n, n, 5)
+    assert (got[0], got[1], got[2]) == (dx, dy, resp)
