@@ -15,8 +15,7 @@ static cudaError_t cols_t(const PassArgs &a, int images, cudaStream_t s) {
         if (e != cudaSuccess) return e;
     }
     dim3 grid((a.cols + W - 1) / W, images);
-    kern<<<grid, threads, smem, s>>>(a);
-    return cudaGetLastError();
+    return launch_pass(kern, grid, threads, smem, s, a);
 }
 
 template <int LD, int ST>

@@ -16,6 +16,7 @@
 #include "fft_config.h"
 #include "fft_device.cuh"
 #include "glsfft_internal.h"
+#include "pdl.cuh"
 #include "spectrum_device.cuh"
 
 namespace glsfft {
@@ -108,36 +109,12 @@ __device__ __forceinline__ void *image_out(const PassArgs &a, unsigned z) {
     return static_cast<char *>(a.out0) + (size_t)z * a.out_img_bytes;
 }
 
-// Programmatic dependent launch.  A pass launched with PassArgs::pdl can be
-// made resident while its stream predecessor is still running; it waits here,
-// before its first global access, until that grid has completed and its
-// memory is visible, then lets its own successor launch.  Both instructions
-// return at once in a grid launched without the attribute.
-__device__ __forceinline__ void pdl_enter() {
-    asm volatile("griddepcontrol.wait;" ::: "memory");
-    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
-}
-
-// Launch one pass kernel, with the programmatic-serialisation attribute when
-// a.pdl is set (the kernel must begin with pdl_enter()).
+// Launch one pass kernel, with programmatic dependent launch when a.pdl is
+// set (the kernel must begin with pdl_enter()).
 template <typename Kern>
 inline cudaError_t launch_pass(Kern kern, dim3 grid, unsigned threads, size_t smem,
                                cudaStream_t s, const PassArgs &a) {
-    if (!a.pdl) {
-        kern<<<grid, threads, smem, s>>>(a);
-        return cudaGetLastError();
-    }
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-    attr[0].val.programmaticStreamSerializationAllowed = 1;
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = grid;
-    cfg.blockDim = dim3(threads);
-    cfg.dynamicSmemBytes = smem;
-    cfg.stream = s;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, kern, a);
+    return launch_maybe_pdl(a.pdl != 0, kern, grid, dim3(threads), smem, s, a);
 }
 
 // ------------------------------------------------------------ load / store
@@ -331,6 +308,7 @@ __global__ void __launch_bounds__(W *LineFft<N, E>::T)
     constexpr int T = F::T;
     extern __shared__ float4 smem_raw[];
     float2 *smem = reinterpret_cast<float2 *>(smem_raw);
+    pdl_enter();
 
     const int c = threadIdx.x % W, t = threadIdx.x / W;
     const int col = blockIdx.x * W + c;

@@ -20,6 +20,7 @@
 #include "fft_device.cuh"
 #include "glsfft.h"
 #include "glsfft_internal.h"
+#include "pdl.cuh"
 #include "spectrum_device.cuh"
 
 using namespace glsfft;
@@ -209,6 +210,7 @@ __global__ void __launch_bounds__(kThreads) minmax_kernel(const float *__restric
 __global__ void __launch_bounds__(kThreads) normalize_kernel(const float *x, float *d, size_t n,
                                                              const unsigned long long *keys,
                                                              double alpha, double beta) {
+    pdl_enter();  // the keys come from the grid before
     const double mn = min_key_value(keys[0]), mx = max_key_value(keys[1]);
     const float scl = __fdiv_rn((float)(beta - alpha), (float)(mx - mn));
     const float c = (float)__dsub_rn(alpha, __dmul_rn((double)scl, mn));
@@ -390,9 +392,10 @@ int glsfft_normalize_minmax(glsfft_context ctx, const float *src, float *dst, in
     if (!st) st = glsfft_min_max_loc_async(ctx, src, rows, cols, keys, stream);
     if (st) return st;
     const size_t n = (size_t)rows * cols;
-    normalize_kernel<<<grid_for(normalize_kernel, n), kThreads, 0, (cudaStream_t)stream>>>(
-        src, dst, n, keys, alpha, beta);
-    return cuda_status(cudaGetLastError());
+    // resident while the min / max pass drains
+    return cuda_status(launch_maybe_pdl(true, normalize_kernel, grid_for(normalize_kernel, n),
+                                        kThreads, 0, (cudaStream_t)stream, src, dst, n,
+                                        (const unsigned long long *)keys, alpha, beta));
 }
 
 int glsfft_fft_display(glsfft_context ctx, const float *frame, const float *window, float *dst,
@@ -423,6 +426,7 @@ int glsfft_fft_display(glsfft_context ctx, const float *frame, const float *wind
     r.flags = PF_SHIFT_COLS;
     r.tw = ctx->d_tw;
     r.key = keys;
+    r.pdl = 1;  // the three launches are chained by programmatic dependent launch
     cudaError_t e = launch_rows(cols, window ? LD_R1W : LD_R1, ST_C2, r, 1, s);
     if (e != cudaSuccess) return cuda_status(e);
     if (rows > 1) {
@@ -439,6 +443,7 @@ int glsfft_fft_display(glsfft_context ctx, const float *frame, const float *wind
         c.param = offset;
         c.err = ctx->d_status;
         c.stall_ns = ctx->stall_ns;
+        c.pdl = 1;  // the plain column kernel; the streamed pass launches as usual
         // 4096-point columns: the streamed pass (TMA-fed, one block per SM)
         e = rows == 4096 && stream_pass_applies(rows, true, c, 1, ST_LOGMAG_MINMAX)
                 ? launch_stream_pass(rows, true, c, 1, s, ST_LOGMAG_MINMAX)
@@ -450,8 +455,9 @@ int glsfft_fft_display(glsfft_context ctx, const float *frame, const float *wind
     }
     if (e != cudaSuccess) return cuda_status(e);
     // normalize(0, 1, NORM_MINMAX) in place
-    normalize_kernel<<<grid_for(normalize_kernel, n), kThreads, 0, s>>>(dst, dst, n, keys, 0.0, 1.0);
-    return cuda_status(cudaGetLastError());
+    return cuda_status(launch_maybe_pdl(true, normalize_kernel, grid_for(normalize_kernel, n),
+                                        kThreads, 0, s, (const float *)dst, dst, n,
+                                        (const unsigned long long *)keys, 0.0, 1.0));
 }
 
 }  // extern "C"
