@@ -193,3 +193,25 @@ def test_fft_display_4096_equals_composed_ops(ctx, torch_cuda):
     torch.cuda.synchronize()
     assert _eq(fused.cpu().numpy(), composed.cpu().numpy())
     assert ctx.device_status() == 0
+
+
+@pytest.mark.parametrize("n", [256, 1024, 4096])
+def test_fft_display_back_to_back_frames(ctx, torch_cuda, n):
+    # frames queued on one stream share the context's spectrum buffer and
+    # min / max keys, and each call's three launches are chained by
+    # programmatic dependent launch: every output must equal the same frame
+    # displayed alone, bit for bit
+    torch = torch_cuda
+    s = stream_handle(torch)
+    win = _dev(torch, wl.hann_window(n, n))
+    frames = [_dev(torch, wl.smooth_field(n, n, seed=300 + i)) for i in range(3 if n == 4096 else 6)]
+    outs = [torch.empty((n, n), dtype=torch.float32, device="cuda") for _ in frames]
+    for f, o in zip(frames, outs):
+        ctx.fft_display(f.data_ptr(), win.data_ptr(), o.data_ptr(), n, n, 1.0, s)
+    torch.cuda.synchronize()
+    got = [o.cpu().numpy() for o in outs]
+    alone = torch.empty((n, n), dtype=torch.float32, device="cuda")
+    for f, g_ in zip(frames, got):
+        ctx.fft_display(f.data_ptr(), win.data_ptr(), alone.data_ptr(), n, n, 1.0, s)
+        torch.cuda.synchronize()
+        assert _eq(g_, alone.cpu().numpy())
