@@ -27,6 +27,8 @@ HEADER_PATHS = sorted((PKG.parent / "include").rglob("*.h"))
 DFT_INVERSE = GLS_FFT_INVERSE = 1
 DFT_SCALE = GLS_FFT_SCALE = 2
 GLS_FFT_SHIFT = 64
+# OR into the algo of phase_correlate_reference: |F1 conj F2| = 0 gives 0, not NaN
+REFERENCE_ZERO_GUARD = 16
 
 _vp = ctypes.c_void_p
 _ip = ctypes.c_int
@@ -95,6 +97,8 @@ _SIGNATURES = {
     "glsfft_server_wait": (_ip, [_vp, ctypes.c_longlong, _dp, _dp, ctypes.c_double]),
     "glsfft_server_replay": (_ip, [_vp, _ip, _dp, ctypes.POINTER(_ip), ctypes.POINTER(_vp), _ip,
                                    _dp, _dp]),
+    "glsfft_server_replay_traced": (_ip, [_vp, _ip, _dp, ctypes.POINTER(_ip), ctypes.POINTER(_vp),
+                                          _ip, _dp, _dp, _dp]),
     "glsfft_server_stats": (_ip, [_vp, ctypes.POINTER(ctypes.c_longlong)]),
     "glsfft_server_destroy": (_ip, [_vp]),
 }
@@ -435,17 +439,25 @@ class Server:
                                        float(timeout_s)), "server_wait")
         return list(res), lat.value
 
-    def replay(self, offsets_s, ref_ids, host_frames, box: int = 5):
+    def replay(self, offsets_s, ref_ids, host_frames, box: int = 5, phases: bool = False):
+        """Open-loop replay; returns (latencies, results) and, with phases,
+        also each request's (late, queued, issuing, device + completion,
+        device time, its copy part) seconds."""
         n = len(offsets_s)
         offs = (ctypes.c_double * n)(*[float(x) for x in offsets_s])
         refs = (_ip * n)(*[int(x) for x in ref_ids])
         frames = (_vp * n)(*[int(x) for x in host_frames])
         lat = (ctypes.c_double * n)()
         res = (ctypes.c_double * (5 * n))()
-        check(lib().glsfft_server_replay(self.handle, n, ctypes.cast(offs, _dp), refs, frames,
-                                         int(box), ctypes.cast(lat, _dp), ctypes.cast(res, _dp)),
+        ph = (ctypes.c_double * (6 * n))()
+        check(lib().glsfft_server_replay_traced(self.handle, n, ctypes.cast(offs, _dp), refs,
+                                                frames, int(box), ctypes.cast(lat, _dp),
+                                                ctypes.cast(res, _dp), ctypes.cast(ph, _dp)),
               "server_replay")
-        return list(lat), [list(res[5 * k:5 * k + 5]) for k in range(n)]
+        out = (list(lat), [list(res[5 * k:5 * k + 5]) for k in range(n)])
+        if phases:
+            return out + ([list(ph[6 * k:6 * k + 6]) for k in range(n)],)
+        return out
 
     def stats(self) -> dict:
         out = (ctypes.c_longlong * 8)()

@@ -58,8 +58,9 @@ static float2 twiddle(long long k, long long n) {
 // ---------------------------------------------- tensor-core form tables
 int glsfft::tc_tables_create(TcTables *t) {
     const size_t f32_halves = 64 * 72, f64_halves = 128 * 136;  // 2N1 x (2N1 + 8)
-    const size_t bytes = 2 * (f32_halves + f64_halves) * sizeof(__half) +
-                         (1024 + 4096) * sizeof(float2) + 256;
+    const size_t dft_off = (2 * (f32_halves + f64_halves) * sizeof(__half) +
+                            (1024 + 4096) * sizeof(float2) + 16 + 1023) / 1024 * 1024;
+    const size_t bytes = dft_off + 16384 + 1024;
     std::vector<unsigned char> host(bytes, 0);
     unsigned char *p = host.data();
     __half *h32 = reinterpret_cast<__half *>(p), *l32 = h32 + f32_halves;
@@ -86,6 +87,14 @@ int glsfft::tc_tables_create(TcTables *t) {
         for (int n2 = 0; n2 < 32; n2++) tw1[k1 * 32 + n2] = twiddle((long long)k1 * n2, 1024);
     for (int k1 = 0; k1 < 64; k1++)
         for (int n2 = 0; n2 < 64; n2++) tw4[k1 * 64 + n2] = twiddle((long long)k1 * n2, 4096);
+    double cs32[32][2];
+    for (int m = 0; m < 32; m++) {
+        double re, im;  // e^{-2 pi i m / 32} = cos - i sin
+        twiddle_d(m, 32, re, im);
+        cs32[m][0] = re;
+        cs32[m][1] = -im;
+    }
+    tc5_dft32_image(cs32, p + dft_off);
     void *d = nullptr;
     cudaError_t e = cudaMalloc(&d, bytes);
     if (e == cudaSuccess) e = cudaMemcpy(d, host.data(), bytes, cudaMemcpyHostToDevice);
@@ -103,6 +112,7 @@ int glsfft::tc_tables_create(TcTables *t) {
     t->f64_lo = reinterpret_cast<__half *>(rebase(l64));
     t->tw1024 = reinterpret_cast<float2 *>(rebase(tw1));
     t->tw4096 = reinterpret_cast<float2 *>(rebase(tw4));
+    t->dft32_sw = b + dft_off;
     return GLSFFT_SUCCESS;
 }
 
@@ -199,6 +209,9 @@ int glsfft::ensure_workspace(glsfft_context ctx, size_t bytes) {
 
 // The two passes of gls::fft over `count` back-to-back images (one launch
 // per pass for the whole batch).  `real_in`: src is CV_32FC1 (promote).
+// Both launches use programmatic dependent launch: the column pass is
+// resident and waiting while the row pass drains, and the row pass of the
+// next call on the stream likewise behind this call's column pass.
 int glsfft::fft2d_launch(glsfft_context ctx, const void *src, void *dst, int rows, int cols,
                          int flags, bool real_in, cudaStream_t s, int count) {
     const bool inv = flags & GLSFFT_INVERSE, scale = flags & GLSFFT_SCALE,
@@ -221,6 +234,7 @@ int glsfft::fft2d_launch(glsfft_context ctx, const void *src, void *dst, int row
         a.stall_ns = ctx->stall_ns;
         a.in_img_bytes = px * (real_in ? sizeof(float) : sizeof(float2));
         a.out_img_bytes = px * sizeof(float2);
+        a.pdl = 1;
         cudaError_t e = real_in ? launch_rows(cols, LD_R1, ST_C2, a, count, s)
                                 : launch_rows_sched(cols, sc.row, a, count, s);
         if (e != cudaSuccess) return cuda_status(e);
@@ -238,6 +252,7 @@ int glsfft::fft2d_launch(glsfft_context ctx, const void *src, void *dst, int row
         a.err = ctx->d_status;
         a.stall_ns = ctx->stall_ns;
         a.in_img_bytes = a.out_img_bytes = px * sizeof(float2);
+        a.pdl = 1;
         cudaError_t e = launch_cols_sched(rows, sc.col, a, count, s);
         if (e != cudaSuccess) return cuda_status(e);
     }

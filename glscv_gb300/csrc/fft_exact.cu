@@ -331,11 +331,16 @@ __global__ void exact_promote_kernel(const float *a, const float *b, const float
     }
 }
 
-// the phase-only spectrum, no epsilon (glsBasicOperation.cpp:195-206)
-__global__ void exact_poc_kernel(float2 *f1, const float2 *f2, size_t n) {
+// the phase-only spectrum, no epsilon (glsBasicOperation.cpp:195-206); with
+// `guard`, a bin whose |F1 conj F2| is 0 gives 0 instead of 0/0 = NaN
+__global__ void exact_poc_kernel(float2 *f1, const float2 *f2, size_t n, int guard) {
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
-         i += (size_t)gridDim.x * blockDim.x)
-        f1[i] = spec_poc(f1[i], f2[i]);
+         i += (size_t)gridDim.x * blockDim.x) {
+        const float2 p = spec_poc(f1[i], f2[i]);
+        const float2 t = spec_mul<true>(f1[i], f2[i]);
+        const bool zero = guard && !(sqrtf(__fadd_rn(__fmul_rn(t.x, t.x), __fmul_rn(t.y, t.y))) > 0.f);
+        f1[i] = zero ? make_float2(0.f, 0.f) : p;
+    }
 }
 
 // the real part (glsPhaseCorrelate.cpp:202-204) and its first-max key
@@ -403,6 +408,8 @@ int glsfft_fft2d_reference(glsfft_context ctx, const void *src, void *dst, int c
 int glsfft_phase_correlate_reference(glsfft_context ctx, const float *src1, const float *src2,
                                      const float *window, int rows, int cols, int box, int algo,
                                      double *dx, double *dy, double *response, void *stream) {
+    const int guard = (algo & GLSFFT_REFERENCE_ZERO_GUARD) ? 1 : 0;
+    algo &= ~GLSFFT_REFERENCE_ZERO_GUARD;
     if (!dx || !dy || (algo != 0 && algo != 1)) return GLSFFT_ERROR_INVALID_VALUE;
     int st = check_poc_args(ctx, src1, src2, window, rows, cols, box);
     if (st) return st;
@@ -426,7 +433,7 @@ int glsfft_phase_correlate_reference(glsfft_context ctx, const float *src1, cons
     st = fft2d_exact_launch(ctx, f1, f1, tmp, 1, rows, cols, 0, algo, s);
     if (!st) st = fft2d_exact_launch(ctx, f2, f2, tmp, 1, rows, cols, 0, algo, s);
     if (st) return st;
-    exact_poc_kernel<<<elem_grid(n), kExactThreads, 0, s>>>(f1, f2, n);
+    exact_poc_kernel<<<elem_grid(n), kExactThreads, 0, s>>>(f1, f2, n, guard);
     e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_status(e);
     // fft(C, C, INVERSE | SHIFT), unscaled (glsPhaseCorrelate.cpp:199)

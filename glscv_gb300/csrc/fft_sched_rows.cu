@@ -20,8 +20,7 @@ static cudaError_t rows_s(const PassArgs &a, int images, cudaStream_t s) {
             if (e != cudaSuccess) return e;
         }
         dim3 grid((a.rows + sh.G - 1) / sh.G, images);
-        kern<<<grid, threads, smem, s>>>(a);
-        return cudaGetLastError();
+        return launch_pass(kern, grid, threads, smem, s, a);
     }
 }
 

@@ -93,6 +93,7 @@ __global__ void __launch_bounds__(stream_threads<N, E>(), 1)
     unsigned long long *full =
         reinterpret_cast<unsigned long long *>(base + kStreamTileBytes + stream_xchg_bytes<N>());
 
+    pdl_enter();  // before the first tile copy reads the input
     const int tid = threadIdx.x;
     const int tpi = a.cols / L;  // tiles per image
     const int total = tpi * images;
@@ -174,8 +175,8 @@ cudaError_t stream_launch(const PassArgs &a, int images, cudaStream_t s) {
     if (sms <= 0) return cudaErrorNotSupported;
     const long long total = (long long)(a.cols / L) * images;
     const int grid = (int)(total < sms ? total : sms);
-    kern<<<grid, stream_threads<N, E>(), smem, s>>>(tmap, a, images);
-    return cudaGetLastError();
+    return launch_maybe_pdl(a.pdl != 0, kern, dim3(grid), dim3(stream_threads<N, E>()), smem, s,
+                            tmap, a, images);
 }
 
 }  // namespace

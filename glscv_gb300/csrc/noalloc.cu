@@ -3,6 +3,7 @@
 // file-scope static device arrays; host code reaches them only through the
 // device addresses cudaGetSymbolAddress returns (the array names are host
 // stand-ins in host code, not device addresses).
+#include <cuda.h>
 #include <cstdint>
 #include <mutex>
 
@@ -21,38 +22,82 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 static __device__ __align__(256) float2 g_noalloc_twiddles[glsfft::kTwEntries];
 
 struct DeviceSetup {
-    bool ready = false;
-    unsigned char *scratch = nullptr;  // device address of g_noalloc_scratch
-    float2 *twiddles = nullptr;        // device address of g_noalloc_twiddles
+    unsigned long long context_id = 0;  // the CUDA context the addresses belong to
+    unsigned char *scratch = nullptr;   // device address of g_noalloc_scratch
+    float2 *twiddles = nullptr;         // device address of g_noalloc_twiddles
 };
 
-constexpr int kMaxDevices = 64;
+// The set-up is cached per CUDA context, not per device ordinal: after a
+// cudaDeviceReset, or on another driver context of the same device, the
+// module's static arrays are fresh (zeroed, possibly at other addresses), so
+// a new context id redoes the address lookup and the twiddle upload.
+constexpr int kMaxContexts = 64;
 std::mutex g_setup_mutex;
-DeviceSetup g_setup[kMaxDevices];
-float2 g_host_twiddles[glsfft::kTwEntries];  // staging for the one upload
+DeviceSetup g_setup[kMaxContexts];
+int g_setup_next = 0;  // round-robin replacement once every entry is used
+float2 g_host_twiddles[glsfft::kTwEntries];  // staging for the upload
 
-// Once per device, with that device current.
-int setup_current_device(DeviceSetup **out) {
+using CtxGetCurrent = CUresult (*)(CUcontext *);
+using CtxGetId = CUresult (*)(CUcontext, unsigned long long *);
+
+void *driver_entry(const char *name, int version) {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion(name, &p, version, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+        return nullptr;
+    return p;
+}
+
+// The id of the calling thread's current CUDA context (0 on failure).
+unsigned long long current_context_id() {
+    static std::once_flag once;
+    static CtxGetCurrent get_current = nullptr;
+    static CtxGetId get_id = nullptr;
+    std::call_once(once, [] {
+        get_current = reinterpret_cast<CtxGetCurrent>(driver_entry("cuCtxGetCurrent", 4000));
+        get_id = reinterpret_cast<CtxGetId>(driver_entry("cuCtxGetId", 12000));
+    });
+    if (!get_current || !get_id) return 0;
+    CUcontext c = nullptr;
+    unsigned long long id = 0;
+    if (get_current(&c) != CUDA_SUCCESS || !c || get_id(c, &id) != CUDA_SUCCESS) return 0;
+    return id;
+}
+
+// Once per CUDA context, with that context current (the current device's
+// primary context for runtime-API callers).
+int setup_current_context(DeviceSetup *out) {
     int dev = -1;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return glsfft::cuda_status(e);
-    if (dev < 0 || dev >= kMaxDevices) return GLSFFT_ERROR_INVALID_VALUE;
     std::lock_guard<std::mutex> lock(g_setup_mutex);
-    DeviceSetup &s = g_setup[dev];
-    if (!s.ready) {
-        void *p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess) return glsfft::cuda_status(e);
-        s.scratch = static_cast<unsigned char *>(p);
-        e = cudaGetSymbolAddress(&p, g_noalloc_twiddles);
-        if (e != cudaSuccess) return glsfft::cuda_status(e);
-        s.twiddles = static_cast<float2 *>(p);
-        glsfft::make_twiddle_host(g_host_twiddles);
-        e = cudaMemcpyToSymbol(g_noalloc_twiddles, g_host_twiddles, sizeof(g_host_twiddles));
-        if (e != cudaSuccess) return glsfft::cuda_status(e);
-        s.ready = true;
-    }
-    *out = &s;
+    unsigned long long id = current_context_id();
+    if (id != 0)
+        for (const DeviceSetup &s : g_setup)
+            if (s.context_id == id) {
+                *out = s;
+                return GLSFFT_SUCCESS;
+            }
+    // the lookup also makes the runtime's primary context current when this
+    // thread has none yet
+    void *p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return glsfft::cuda_status(e);
+    DeviceSetup s;
+    s.scratch = static_cast<unsigned char *>(p);
+    e = cudaGetSymbolAddress(&p, g_noalloc_twiddles);
+    if (e != cudaSuccess) return glsfft::cuda_status(e);
+    s.twiddles = static_cast<float2 *>(p);
+    glsfft::make_twiddle_host(g_host_twiddles);
+    e = cudaMemcpyToSymbol(g_noalloc_twiddles, g_host_twiddles, sizeof(g_host_twiddles));
+    if (e != cudaSuccess) return glsfft::cuda_status(e);
+    if (id == 0) id = current_context_id();
+    if (id == 0) return GLSFFT_ERROR_CUDA;
+    s.context_id = id;
+    g_setup[g_setup_next] = s;
+    g_setup_next = (g_setup_next + 1) % kMaxContexts;
+    *out = s;
     return GLSFFT_SUCCESS;
 }
 
@@ -73,9 +118,10 @@ extern "C" int glsfft_phase_correlate_noalloc(const float *src1, const float *sr
         (window && (reinterpret_cast<uintptr_t>(window) & 3)) ||
         (reinterpret_cast<uintptr_t>(d_result) & 7))
         return GLSFFT_ERROR_MISALIGNED;
-    DeviceSetup *s = nullptr;
-    int st = setup_current_device(&s);
+    DeviceSetup setup;
+    int st = setup_current_context(&setup);
     if (st) return st;
+    const DeviceSetup *s = &setup;
     float2 *f1 = reinterpret_cast<float2 *>(s->scratch);
     float2 *f2 = f1 + n;
     float *surface = reinterpret_cast<float *>(f2 + n);

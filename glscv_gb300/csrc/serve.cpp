@@ -53,17 +53,25 @@ struct Request {
     int ref = 0;
     const float *frame = nullptr;  // host pointer, valid until completion
     int box = 5;
-    Clock::time_point arrival, done_at;
+    // arrival: the scheduled arrival (latency counts from it); submitted: when
+    // the request was queued; admitted: when a dispatcher took a slot and
+    // workspace for it; launched: when its pipeline and event were issued;
+    // done_at: when the poller saw the event complete
+    Clock::time_point arrival, submitted, admitted, launched, done_at;
     int state = REQ_QUEUED;
     int status = GLSFFT_SUCCESS;
     int slot = -1;
     size_t ws_off = Arena::kFail;
     double result[5] = {0, 0, 0, 0, 0};
+    double gpu_s = 0.0;   // device time from the start event to the done event
+    double copy_s = 0.0;  // of which the frame's host-to-device copy
 };
 
 struct Slot {
     cudaStream_t stream = nullptr;
-    cudaEvent_t done = nullptr;
+    cudaEvent_t start = nullptr;   // recorded before the frame's copy (timing)
+    cudaEvent_t copied = nullptr;  // recorded after the frame's copy (timing)
+    cudaEvent_t done = nullptr;   // recorded after the last launch (timing)
     double *h_result = nullptr;      // pinned and mapped, 8 doubles
     double *h_result_dev = nullptr;  // its device-side address
     long long ticket = -1;
@@ -121,7 +129,9 @@ int launch_request(glsfft_server srv, const Reference &ref, const Request &rq, S
     // five calls: the frame's upload, three launches (the POC column pass
     // zeroes the argmax key; the last block of the inverse row pass computes
     // the centroid and writes it into the slot's mapped pinned buffer), the event
-    cudaError_t e = cudaMemcpyAsync(frame, rq.frame, 4 * n, cudaMemcpyHostToDevice, s);
+    cudaError_t e = cudaEventRecord(slot.start, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(frame, rq.frame, 4 * n, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaEventRecord(slot.copied, s);
     if (e != cudaSuccess) return cuda_status(e);
     PassArgs a{};
     a.in0 = frame;
@@ -190,6 +200,7 @@ void dispatcher_main(glsfft_server srv) {
             rq.ws_off = off;
             rq.slot = free_slot;
             rq.state = REQ_RUNNING;
+            rq.admitted = Clock::now();
             Slot &slot = srv->slots[free_slot];
             slot.ticket = ticket;
             slot.launched = false;  // not pollable until its event is recorded
@@ -212,6 +223,7 @@ void dispatcher_main(glsfft_server srv) {
                 srv->failed++;
                 srv->cv_done.notify_all();
             } else {
+                srv->reqs[ticket].launched = Clock::now();
                 srv->slots[free_slot].launched = true;
             }
             srv->cv_poll.notify_one();
@@ -261,6 +273,9 @@ void poller_main(glsfft_server srv) {
             rq.done_at = Clock::now();
             if (state[w] == cudaSuccess) {
                 std::memcpy(rq.result, slot.h_result, sizeof(rq.result));
+                float ms = 0.f;
+                if (cudaEventElapsedTime(&ms, slot.start, slot.done) == cudaSuccess) rq.gpu_s = 1e-3 * ms;
+                if (cudaEventElapsedTime(&ms, slot.start, slot.copied) == cudaSuccess) rq.copy_s = 1e-3 * ms;
                 rq.state = REQ_DONE;
                 srv->completed++;
             } else {
@@ -289,10 +304,33 @@ long long submit_locked(glsfft_server srv, int ref_id, const float *frame, int b
     rq.frame = frame;
     rq.box = box;
     rq.arrival = arrival;
+    rq.submitted = Clock::now();
     srv->reqs.emplace(ticket, rq);
     srv->queue.push_back(ticket);
     srv->peak_queue = std::max<long long>(srv->peak_queue, (long long)srv->queue.size());
     return ticket;
+}
+
+// Wait (at most timeout_s) for a ticket and take its record out of the table.
+int take_request(glsfft_server srv, long long ticket, double timeout_s, Request *out) {
+    std::unique_lock<std::mutex> lock(srv->mu);
+    auto it = srv->reqs.find(ticket);
+    if (it == srv->reqs.end()) return GLSFFT_ERROR_INVALID_VALUE;
+    const auto deadline = Clock::now() + std::chrono::duration_cast<Clock::duration>(
+                                             std::chrono::duration<double>(timeout_s));
+    while (it->second.state < REQ_DONE) {
+        if (srv->cv_done.wait_until(lock, deadline) == std::cv_status::timeout &&
+            it->second.state < REQ_DONE)
+            return GLSFFT_ERROR_TIMEOUT;
+        it = srv->reqs.find(ticket);
+    }
+    *out = it->second;
+    srv->reqs.erase(it);
+    return GLSFFT_SUCCESS;
+}
+
+double seconds(Clock::time_point a, Clock::time_point b) {
+    return std::chrono::duration<double>(b - a).count();
 }
 
 }  // namespace
@@ -318,13 +356,17 @@ int glsfft_server_create(glsfft_context ctx, int slots, size_t hbm_budget, glsff
     srv->slots.resize(slots);
     for (auto &s : srv->slots) {
         cudaError_t e = cudaStreamCreateWithFlags(&s.stream, cudaStreamNonBlocking);
-        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s.done, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreate(&s.start);
+        if (e == cudaSuccess) e = cudaEventCreate(&s.copied);
+        if (e == cudaSuccess) e = cudaEventCreate(&s.done);
         if (e == cudaSuccess) e = cudaHostAlloc(&s.h_result, 8 * sizeof(double), cudaHostAllocMapped);
         if (e == cudaSuccess) e = cudaHostGetDevicePointer(&s.h_result_dev, s.h_result, 0);
         if (e != cudaSuccess) {
             cudaGetLastError();
             for (auto &t : srv->slots) {
                 if (t.stream) cudaStreamDestroy(t.stream);
+                if (t.start) cudaEventDestroy(t.start);
+                if (t.copied) cudaEventDestroy(t.copied);
                 if (t.done) cudaEventDestroy(t.done);
                 if (t.h_result) cudaFreeHost(t.h_result);
             }
@@ -416,27 +458,17 @@ int glsfft_server_submit(glsfft_server srv, int ref_id, const float *host_frame,
 int glsfft_server_wait(glsfft_server srv, long long ticket, double *result5, double *latency_s,
                        double timeout_s) {
     if (!srv) return GLSFFT_ERROR_INVALID_VALUE;
-    std::unique_lock<std::mutex> lock(srv->mu);
-    auto it = srv->reqs.find(ticket);
-    if (it == srv->reqs.end()) return GLSFFT_ERROR_INVALID_VALUE;
-    const auto deadline = Clock::now() + std::chrono::duration_cast<Clock::duration>(
-                                             std::chrono::duration<double>(timeout_s));
-    while (it->second.state < REQ_DONE) {
-        if (srv->cv_done.wait_until(lock, deadline) == std::cv_status::timeout &&
-            it->second.state < REQ_DONE)
-            return GLSFFT_ERROR_TIMEOUT;
-        it = srv->reqs.find(ticket);
-    }
-    const Request rq = it->second;
-    srv->reqs.erase(it);
+    Request rq;
+    const int st = take_request(srv, ticket, timeout_s, &rq);
+    if (st) return st;
     if (result5) std::memcpy(result5, rq.result, sizeof(rq.result));
-    if (latency_s) *latency_s = std::chrono::duration<double>(rq.done_at - rq.arrival).count();
+    if (latency_s) *latency_s = seconds(rq.arrival, rq.done_at);
     return rq.state == REQ_DONE ? GLSFFT_SUCCESS : rq.status;
 }
 
-int glsfft_server_replay(glsfft_server srv, int n, const double *offsets_s, const int *ref_ids,
-                         const float *const *host_frames, int box, double *latencies_s,
-                         double *results5) {
+int glsfft_server_replay_traced(glsfft_server srv, int n, const double *offsets_s,
+                                const int *ref_ids, const float *const *host_frames, int box,
+                                double *latencies_s, double *results5, double *phases6) {
     if (!srv || n < 1 || !offsets_s || !ref_ids || !host_frames || !latencies_s || box < 1)
         return GLSFFT_ERROR_INVALID_VALUE;
     {
@@ -451,12 +483,16 @@ int glsfft_server_replay(glsfft_server srv, int n, const double *offsets_s, cons
     std::vector<long long> tickets(n);
     const Clock::time_point t0 = Clock::now();
     for (int k = 0; k < n; k++) {
-        // open-loop arrivals: latency counts from the scheduled arrival time
+        // open-loop arrivals: latency counts from the scheduled arrival time.
+        // Sleep while more than 300 us remain (a sleep can overrun by tens of
+        // microseconds), then poll the clock.
         const Clock::time_point at =
             t0 + std::chrono::duration_cast<Clock::duration>(std::chrono::duration<double>(offsets_s[k]));
-        while (Clock::now() < at) {
+        for (;;) {
             const auto left = at - Clock::now();
-            if (left > std::chrono::microseconds(200)) std::this_thread::sleep_for(left / 2);
+            if (left <= Clock::duration::zero()) break;
+            if (left > std::chrono::microseconds(300))
+                std::this_thread::sleep_for(left - std::chrono::microseconds(250));
         }
         std::lock_guard<std::mutex> lock(srv->mu);
         tickets[k] = submit_locked(srv, ref_ids[k], host_frames[k], box, at);
@@ -464,12 +500,30 @@ int glsfft_server_replay(glsfft_server srv, int n, const double *offsets_s, cons
     }
     int status = GLSFFT_SUCCESS;
     for (int k = 0; k < n; k++) {
-        double r[5];
-        const int st = glsfft_server_wait(srv, tickets[k], r, &latencies_s[k], 60.0);
+        Request rq;
+        int st = take_request(srv, tickets[k], 60.0, &rq);
+        if (!st && rq.state != REQ_DONE) st = rq.status;
         if (st && !status) status = st;
-        if (results5) std::memcpy(results5 + 5 * (size_t)k, r, sizeof(r));
+        latencies_s[k] = st ? -1.0 : seconds(rq.arrival, rq.done_at);
+        if (results5) std::memcpy(results5 + 5 * (size_t)k, rq.result, sizeof(rq.result));
+        if (phases6) {
+            double *ph = phases6 + 6 * (size_t)k;
+            ph[0] = seconds(rq.arrival, rq.submitted);   // arrival thread's lateness
+            ph[1] = seconds(rq.submitted, rq.admitted);  // queued: slot / workspace / dispatcher
+            ph[2] = seconds(rq.admitted, rq.launched);   // issuing the copy, launches, events
+            ph[3] = seconds(rq.launched, rq.done_at);    // device work + completion polling
+            ph[4] = rq.gpu_s;                            // device time, start to done event
+            ph[5] = rq.copy_s;                           // of which the frame's copy
+        }
     }
     return status;
+}
+
+int glsfft_server_replay(glsfft_server srv, int n, const double *offsets_s, const int *ref_ids,
+                         const float *const *host_frames, int box, double *latencies_s,
+                         double *results5) {
+    return glsfft_server_replay_traced(srv, n, offsets_s, ref_ids, host_frames, box, latencies_s,
+                                       results5, nullptr);
 }
 
 int glsfft_server_stats(glsfft_server srv, long long *out8) {
@@ -511,6 +565,8 @@ int glsfft_server_destroy(glsfft_server srv) {
             cudaStreamSynchronize(s.stream);
             cudaStreamDestroy(s.stream);
         }
+        if (s.start) cudaEventDestroy(s.start);
+        if (s.copied) cudaEventDestroy(s.copied);
         if (s.done) cudaEventDestroy(s.done);
         if (s.h_result) cudaFreeHost(s.h_result);
     }

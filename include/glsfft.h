@@ -154,7 +154,12 @@ GLSFFT_API int glsfft_fft2d_reference(glsfft_context ctx, const void *src, void 
  * epsilon (0/0 -> NaN, as the reference), unscaled inverse with the quadrant
  * shift, real part, first-max location, FP64 centroid; synchronous.  Every
  * step rounds as the reference's CPU code, so dx, dy and response are
- * bit-identical to it on the same inputs. */
+ * bit-identical to it on the same inputs.  `algo` is 0 or 1 as above,
+ * optionally ORed with GLSFFT_REFERENCE_ZERO_GUARD: a bin whose
+ * |F1 conj(F2)| is exactly 0 then gives 0 instead of 0/0 = NaN (the default
+ * path's behaviour; smooth inputs such as a blurred field hit such bins, and
+ * one NaN poisons the reference's whole surface). */
+#define GLSFFT_REFERENCE_ZERO_GUARD 16
 GLSFFT_API int glsfft_phase_correlate_reference(glsfft_context ctx, const float *src1,
                                                 const float *src2, const float *window, int rows,
                                                 int cols, int box, int algo, double *dx,
@@ -479,6 +484,8 @@ GLSFFT_API int glsfft_server_create(glsfft_context ctx, int slots, size_t hbm_bu
  * Make a reference resident: its spectrum FFT2(window x frame) is computed
  * once (frame, window: CV_32FC1 device images; window may be NULL) and
  * kept in the server's budget.  Synchronous.  Returns its id in *ref_id.
+ * The server reads frame and window on its own stream: work that produces
+ * them on another stream must be complete before the call.
  */
 GLSFFT_API int glsfft_server_add_reference(glsfft_server server, const float *frame,
                                            const float *window, int rows, int cols, int *ref_id);
@@ -511,6 +518,23 @@ GLSFFT_API int glsfft_server_replay(glsfft_server server, int n, const double *o
                                     const int *ref_ids, const float *const *host_frames, int box,
                                     double *latencies_s, double *results5);
 
+/*
+ * glsfft_server_replay that also attributes each request's latency (no
+ * reference counterpart): phases6[6k .. 6k+3] = seconds from the scheduled
+ * arrival to the actual submission (the arrival thread's lateness), queued
+ * (waiting for a slot, workspace or a dispatcher), issuing (the frame's
+ * copy, the three launches and the events), and device work plus
+ * completion polling -- these four sum to latencies_s[k] -- then
+ * phases6[6k+4] = the device time between events recorded before the copy
+ * and after the last launch (so phase 3 minus it is the completion lag) and
+ * phases6[6k+5] = the part of it up to the end of the frame's copy.
+ * phases6 may be NULL.
+ */
+GLSFFT_API int glsfft_server_replay_traced(glsfft_server server, int n, const double *offsets_s,
+                                           const int *ref_ids, const float *const *host_frames,
+                                           int box, double *latencies_s, double *results5,
+                                           double *phases6);
+
 /* Counters: admitted, completed, failed, peak in flight, peak queue length,
  * budget bytes, peak budget bytes in use, resident references. */
 GLSFFT_API int glsfft_server_stats(glsfft_server server, long long *out8);
@@ -541,9 +565,12 @@ GLSFFT_API int glsfft_server_destroy(glsfft_server server);
  * array (5 MiB) and a 256 KiB twiddle table are held on every GPU that loads
  * the library until the process exits.
  *
- * The first call on a device (the current device) sets up: it looks up the
- * arrays' device addresses and uploads the twiddle table with a synchronous
- * copy; make that first call before any stream capture.  Every call uses the
+ * The first call in a CUDA context (the current device's, for runtime-API
+ * callers) sets up: it looks up the arrays' device addresses and uploads
+ * the twiddle table with a synchronous copy; make that first call before
+ * any stream capture.  The set-up is remembered per context, so after a
+ * cudaDeviceReset the next call sets up again (and must again come before
+ * any capture).  Every call uses the
  * same scratch array, which keeps the previous call's contents (the argmax
  * word is cleared on each call), so calls whose work overlaps on the GPU --
  * on different streams or from different host threads -- race: issue them

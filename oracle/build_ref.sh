@@ -11,10 +11,14 @@
 #   2. `n = n++` -> `n++` in the butterfly loops: under g++ that statement
 #      leaves n unchanged, so those loops would never end.
 #
-# Usage: oracle/build_ref.sh [REFERENCE_ROOT]   (default /root/reference)
+# Usage: oracle/build_ref.sh REFERENCE_ROOT   (or GLS_REFERENCE_ROOT set)
 set -euo pipefail
 here="$(cd "$(dirname "$0")" && pwd)"
-ref="${1:-/root/reference}"
+ref="${1:-${GLS_REFERENCE_ROOT:-}}"
+if [ -z "$ref" ]; then
+    echo "build_ref: pass the glsCV checkout or set GLS_REFERENCE_ROOT" >&2
+    exit 2
+fi
 src="$ref/UnitTest_glsCV/fft_stockhum.cpp"
 out="$here/_ref"
 if [ ! -f "$src" ]; then

@@ -49,12 +49,26 @@ def build(force: bool = False) -> Path:
     return LIB_PATH
 
 
-def build_ref(reference_root: str = "/root/reference") -> Path | None:
-    """Build oracle/_ref from the reference checkout when it is present."""
+REFERENCE_ENV = "GLS_REFERENCE_ROOT"
+
+
+def reference_root() -> str | None:
+    """The glsCV checkout named by the GLS_REFERENCE_ROOT environment
+    variable, or None when it is unset or holds no fft_stockhum.cpp."""
+    root = os.environ.get(REFERENCE_ENV)
+    if root and Path(root, "UnitTest_glsCV", "fft_stockhum.cpp").exists():
+        return root
+    return None
+
+
+def build_ref(reference_root_dir: str | None = None) -> Path | None:
+    """Build oracle/_ref from a glsCV checkout (the argument, else
+    GLS_REFERENCE_ROOT) when one is present; None otherwise."""
     script = HERE / "build_ref.sh"
-    if not Path(reference_root, "UnitTest_glsCV", "fft_stockhum.cpp").exists():
+    root = reference_root_dir or reference_root()
+    if not root or not Path(root, "UnitTest_glsCV", "fft_stockhum.cpp").exists():
         return None
-    subprocess.check_call(["bash", str(script), reference_root],
+    subprocess.check_call(["bash", str(script), root],
                           stdout=subprocess.DEVNULL)
     return REF_LIB_PATH
 
@@ -307,3 +321,54 @@ def fft_eps(n: int, flags: int) -> float:
     if not (flags & DFT_SCALE):
         eps *= n
     return np.float32(eps).item()
+
+
+def phase_correlate_f64(a: np.ndarray, b: np.ndarray, window: np.ndarray | None = None,
+                        box: int = 5, zero_guard: bool = True, want_surface: bool = False):
+    """gls::phaseCorrelate (glsCV/glsPhaseCorrelate.cpp:142-231) restated in
+    FP64 / complex128 on the same float32 inputs: window product (exact in
+    FP64), forward 2-D DFTs (numpy pocketfft), phase-only cross spectrum
+    F1 conj(F2) / |F1 conj(F2)| (glsBasicOperation.cpp:195-206; with
+    zero_guard a bin with |.| = 0 becomes 0 instead of 0/0), unscaled inverse
+    with the quadrant shift (:199), real part (:202-204), first maximum in
+    row-major order (glsMinMaxLoc.cpp:65-119), clamped-box weighted centroid
+    with DBL_EPSILON (:60-137), shift = center - centroid and response =
+    sum / (rows*cols) (:219-231).  Returns ((dx, dy), response, peak,
+    surface or None); the surface is float64."""
+    a64 = np.asarray(a, dtype=np.float32).astype(np.float64)
+    b64 = np.asarray(b, dtype=np.float32).astype(np.float64)
+    if window is not None:
+        w64 = np.asarray(window, dtype=np.float32).astype(np.float64)
+        a64, b64 = a64 * w64, b64 * w64
+    rows, cols = a64.shape
+    f1 = np.fft.fft2(a64)
+    f2 = np.fft.fft2(b64)
+    t = f1 * np.conj(f2)
+    mag = np.abs(t)
+    with np.errstate(invalid="ignore", divide="ignore"):
+        p = t / mag
+    if zero_guard:
+        p[~(mag > 0)] = 0.0
+    # unscaled inverse = rows*cols * ifft2, then the quadrant swap
+    c = np.fft.ifft2(p) * (rows * cols)
+    c = np.roll(c, (rows // 2, cols // 2), axis=(0, 1))
+    re = np.ascontiguousarray(c.real)
+    # first maximum in row-major order (NaN never wins)
+    flat = np.where(np.isnan(re), -np.inf, re).ravel()
+    idx = int(np.argmax(flat))
+    py, px = divmod(idx, cols)
+    h = box >> 1
+    minr, maxr = max(py - h, 0), min(py + h, rows - 1)
+    minc, maxc = max(px - h, 0), min(px + h, cols - 1)
+    sx = sy = s = 0.0
+    for y in range(minr, maxr + 1):
+        for x in range(minc, maxc + 1):
+            v = float(re[y, x])
+            sx += x * v
+            sy += y * v
+            s += v
+    response = s / (rows * cols)
+    s += np.finfo(np.float64).eps
+    dx = cols / 2.0 - sx / s
+    dy = rows / 2.0 - sy / s
+    return (dx, dy), response, (px, py), (re if want_surface else None)

@@ -3,11 +3,14 @@
 * White-spectrum inputs (the reference test's uniform images,
   UnitTest_glsPhaseCorrelate.cpp:87): integer peak identical to the oracle's,
   sub-pixel shift within 1e-3 px of the oracle, response within 1e-4.
-* Smooth-field inputs (Gaussian-blurred noise): bins where src1 carries no
-  energy hold FP32 rounding noise, which the phase-only normalisation lifts
-  to unit magnitude with an implementation-specific phase; the integer peak
-  is still identical and must equal the true shift, while the sub-pixel
-  value is compared with a 0.05 px tolerance.
+* Smooth-field inputs (Gaussian-blurred noise, the benchmark configuration):
+  on about 46% of the bins of src1's spectrum any FP32 FFT's rounding error
+  exceeds the bin's own magnitude, and the phase-only normalisation lifts
+  those bins to unit magnitude with an implementation-specific phase.  The
+  integer peak is still identical and must equal the true shift; the
+  sub-pixel value is compared with the FP64 restatement of the whole
+  pipeline over 8 seeds, against the distance the reference's own FP32
+  arithmetic (the oracle) keeps from it.
 * The ground truth (the synthetic shift) is met within the reference test's
   0.25 px (UnitTest_glsPhaseCorrelate.cpp:128-132).
 """
@@ -56,14 +59,14 @@ def test_subpixel_and_box(ctx, torch_cuda, oracle, box):
     assert abs(gresp - oresp) < 1e-4
 
 
-@pytest.mark.parametrize("n,max_shift", [(512, 30), (1024, 100), (2048, 100)])
+@pytest.mark.parametrize("n,max_shift", [(512, 30), (2048, 100)])
 def test_smooth_field_config2b(ctx, torch_cuda, oracle, n, max_shift):
     """A = blurred noise (sigma 4 px) in [0,1], B = A rolled by an integer
-    shift in [-max_shift, max_shift] + N(0, 0.01^2), Hann window (1024 with
-    +-100 px is the benchmark workload).  The shift range is kept where the
-    surface's highest value clears its neighbours by more than the FP32
-    noise floor: at 512 with a 45 px shift the top two values are 2% apart
-    and the FP32 restatement itself picks the wrong neighbour."""
+    shift in [-max_shift, max_shift] + N(0, 0.01^2), Hann window.  The shift
+    range is kept where the surface's highest value clears its neighbours by
+    more than the FP32 noise floor: at 512 with a 45 px shift the top two
+    values are 2% apart and the FP32 restatement itself picks the wrong
+    neighbour."""
     a, b, (dx, dy) = wl.shifted_pair(n, n, seed_field=6, seed_shift=7, max_shift=max_shift)
     win = wl.hann_window(n, n)
     (ox, oy), oresp, opeak, _ = oracle.phase_correlate(a, b, win, box=5)
@@ -71,8 +74,43 @@ def test_smooth_field_config2b(ctx, torch_cuda, oracle, n, max_shift):
                                                  want_surface=True)
     (px, py), _ = oracle.max_loc(gsurf)
     assert (px, py) == opeak == _peak(n, n, dx, dy)
-    assert abs(gx - ox) < 0.05 and abs(gy - oy) < 0.05
+    # two FP32 implementations on a smooth field: see the 1024 test below
+    assert abs(gx - ox) < 0.02 and abs(gy - oy) < 0.02
     assert abs(gx - dx) < 0.25 and abs(gy - dy) < 0.25
+
+
+CONFIG_2B_SEEDS = [(6 + 100 * k, 7 + 100 * k) for k in range(8)]
+
+
+def test_config2b_1024_against_fp64_pipeline(ctx, torch_cuda, oracle):
+    """The benchmark phaseCorrelate (1024^2, shifts in [-100, 100], Hann
+    window), 8 seeds, against the FP64 restatement of the whole pipeline
+    (oracle.phase_correlate_f64: window product, complex128 DFTs, phase-only
+    spectrum with the zero-bin guard, unscaled inverse, first maximum, FP64
+    centroid).  Per seed: the integer peak equals the oracle's, the FP64
+    pipeline's and the true shift; the sub-pixel shift is within 0.01 px of
+    the oracle (measured: at most 0.0062 px over 12 seeds) and within 0.025 px
+    of FP64 (the reference's FP32 arithmetic itself reaches 0.0173 px).  Over
+    the seeds: the GPU's mean distance to FP64 is at most 1.25x the oracle's
+    (measured 0.85x over these 8 seeds: the GPU is on average nearer to FP64
+    than the reference's own FP32 arithmetic)."""
+    torch = torch_cuda
+    n = 1024
+    win = wl.hann_window(n, n)
+    d_gpu, d_orc = [], []
+    for sf, ss in CONFIG_2B_SEEDS:
+        a, b, (dx, dy) = wl.shifted_pair(n, n, seed_field=sf, seed_shift=ss, max_shift=100)
+        (ox, oy), _, opeak, _ = oracle.phase_correlate(a, b, win, box=5)
+        (fx, fy), _, fpeak, _ = oracle.phase_correlate_f64(a, b, win, box=5)
+        (gx, gy), _, gsurf = gpu_phase_correlate(ctx, torch, a, b, win, box=5, want_surface=True)
+        (px, py), _ = oracle.max_loc(gsurf)
+        assert (px, py) == opeak == fpeak == _peak(n, n, dx, dy), (sf, ss)
+        assert max(abs(gx - ox), abs(gy - oy)) <= 0.01, (sf, ss, (gx, gy), (ox, oy))
+        dg = max(abs(gx - fx), abs(gy - fy))
+        assert dg <= 0.025, (sf, ss, dg)
+        d_gpu.append(dg)
+        d_orc.append(max(abs(ox - fx), abs(oy - fy)))
+    assert np.mean(d_gpu) <= 1.25 * np.mean(d_orc), (d_gpu, d_orc)
 
 
 def test_identical_images_zero_shift(ctx, torch_cuda):

@@ -107,3 +107,31 @@ def test_reference_mode_rejects_bad_algo(tctx, torch_cuda):
     d = torch.zeros(16, 16, dtype=torch.complex64, device="cuda")
     with pytest.raises(g.GlsError):
         tctx.fft2d_reference(d.data_ptr(), d.data_ptr(), 16, 16, 0, 2)
+
+
+CONFIG_2B_SEEDS = [(6 + 100 * k, 7 + 100 * k) for k in range(8)]
+
+
+@pytest.mark.parametrize("algo", [0, 1])
+def test_reference_phase_correlate_zero_guard_config2b(tctx, torch_cuda, oracle, algo):
+    """The benchmark phaseCorrelate configuration: 1024^2 smooth field
+    (blurred noise, sigma 4 px), B = A rolled by an integer in [-100, 100]
+    plus N(0, 0.01^2), Hann window, 8 seeds.  Its spectrum has bins where
+    |F1 conj F2| is exactly 0 in FP32, so the reference's epsilon-free
+    phase-only step returns NaN everywhere; with GLSFFT_REFERENCE_ZERO_GUARD
+    those bins become 0 and the reference-arithmetic GPU path equals the
+    oracle's guarded restatement bit for bit (dx, dy, response): 0 px."""
+    torch = torch_cuda
+    n = 1024
+    w = wl.hann_window(n, n)
+    dw = torch.from_numpy(w).cuda()
+    for sf, ss in CONFIG_2B_SEEDS:
+        a, b, (dx, dy) = wl.shifted_pair(n, n, seed_field=sf, seed_shift=ss, max_shift=100)
+        (ox, oy), oresp, opeak, _ = oracle.phase_correlate(a, b, w, box=5, algo=algo,
+                                                           zero_guard=True)
+        da, db = torch.from_numpy(a).cuda(), torch.from_numpy(b).cuda()
+        (gx, gy), gresp = tctx.phase_correlate_reference(
+            da.data_ptr(), db.data_ptr(), dw.data_ptr(), n, n, 5,
+            algo | g.REFERENCE_ZERO_GUARD, stream_handle(torch))
+        assert (gx, gy, gresp) == (ox, oy, oresp), (sf, ss)
+        assert opeak == ((n // 2 - int(dx)) % n, (n // 2 - int(dy)) % n)

@@ -6,9 +6,11 @@ an allocation would synchronise the device.  Its scratch is a static device
 array of the library, shared by every call.  The test calls it through the C
 ABI twice in a row (a larger image, then a smaller one, so the second call
 runs on a scratch array still holding the first call's data) and checks each
-result against the context-based entry point within the tolerance of the other
-phaseCorrelate tests.  It also checks that an image above the static limit is
-refused.  This file sorts last so a failing run has already run every other
+result against the context-based entry point: both run the same kernels with
+the same twiddle table and scratch layout, so dx, dy, response, peak index and
+peak value must be bit-identical (a stale-scratch or layout bug would move
+them).  The integer peak must also equal the oracle's.  It also checks that
+an image above the static limit is refused.  This file sorts last so a failing run has already run every other
 test; it passes alone or after them.
 """
 from __future__ import annotations
@@ -48,7 +50,7 @@ def _with_context(torch, a, b, w, box=5):
     return res.cpu().numpy()
 
 
-def test_noalloc_matches_context_entry_point_two_calls(native, torch_cuda):
+def test_noalloc_matches_context_entry_point_two_calls(native, torch_cuda, oracle):
     torch = torch_cuda
     cases = [((512, 512), 41, (-40.4, 22.7), True), ((256, 256), 42, (17.0, -9.0), False)]
     for (rows, cols), seed, shift, use_window in cases:
@@ -59,9 +61,11 @@ def test_noalloc_matches_context_entry_point_two_calls(native, torch_cuda):
         got = _noalloc(native, torch, da, db, dw)
         ref = _with_context(torch, da, db, dw)
         assert np.all(np.isfinite(got[:5]))
-        assert int(got[3]) == int(ref[3])                       # integer peak
-        assert abs(got[0] - ref[0]) < 1e-3 and abs(got[1] - ref[1]) < 1e-3
-        assert abs(got[2] - ref[2]) < 1e-4
+        # dx, dy, response, peak index, peak value: bit for bit
+        assert np.array_equal(got[:5].view(np.uint64), ref[:5].view(np.uint64)), (got, ref)
+        # the integer peak is the oracle's
+        _, _, (px, py), _ = oracle.phase_correlate(a, b, w, box=5)
+        assert int(got[3]) == py * cols + px
         assert abs(got[0] - shift[0]) < 0.5 and abs(got[1] - shift[1]) < 0.5
 
 
