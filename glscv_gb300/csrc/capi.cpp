@@ -60,7 +60,8 @@ int glsfft::tc_tables_create(TcTables *t) {
     const size_t f32_halves = 64 * 72, f64_halves = 128 * 136;  // 2N1 x (2N1 + 8)
     const size_t dft_off = (2 * (f32_halves + f64_halves) * sizeof(__half) +
                             (1024 + 4096) * sizeof(float2) + 16 + 1023) / 1024 * 1024;
-    const size_t bytes = dft_off + 16384 + 1024;
+    const size_t dft64_off = dft_off + 16384;
+    const size_t bytes = dft64_off + 49152 + 1024;
     std::vector<unsigned char> host(bytes, 0);
     unsigned char *p = host.data();
     __half *h32 = reinterpret_cast<__half *>(p), *l32 = h32 + f32_halves;
@@ -87,14 +88,16 @@ int glsfft::tc_tables_create(TcTables *t) {
         for (int n2 = 0; n2 < 32; n2++) tw1[k1 * 32 + n2] = twiddle((long long)k1 * n2, 1024);
     for (int k1 = 0; k1 < 64; k1++)
         for (int n2 = 0; n2 < 64; n2++) tw4[k1 * 64 + n2] = twiddle((long long)k1 * n2, 4096);
-    double cs32[32][2];
-    for (int m = 0; m < 32; m++) {
-        double re, im;  // e^{-2 pi i m / 32} = cos - i sin
-        twiddle_d(m, 32, re, im);
-        cs32[m][0] = re;
-        cs32[m][1] = -im;
+    double cs[64][2];
+    for (int n1 = 32; n1 <= 64; n1 *= 2) {
+        for (int m = 0; m < n1; m++) {
+            double re, im;  // e^{-2 pi i m / n1} = cos - i sin
+            twiddle_d(m, n1, re, im);
+            cs[m][0] = re;
+            cs[m][1] = -im;
+        }
+        tc5_dft_image(n1, cs, p + (n1 == 32 ? dft_off : dft64_off));
     }
-    tc5_dft32_image(cs32, p + dft_off);
     void *d = nullptr;
     cudaError_t e = cudaMalloc(&d, bytes);
     if (e == cudaSuccess) e = cudaMemcpy(d, host.data(), bytes, cudaMemcpyHostToDevice);
@@ -113,6 +116,7 @@ int glsfft::tc_tables_create(TcTables *t) {
     t->tw1024 = reinterpret_cast<float2 *>(rebase(tw1));
     t->tw4096 = reinterpret_cast<float2 *>(rebase(tw4));
     t->dft32_sw = b + dft_off;
+    t->dft64_sw = b + dft64_off;
     return GLSFFT_SUCCESS;
 }
 

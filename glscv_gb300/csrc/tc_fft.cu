@@ -246,7 +246,7 @@ cudaError_t tc_launch(const PassArgs &a, const TcTables &t, int images, cudaStre
 
 cudaError_t launch_tc_lines(int n, bool rows, const PassArgs &a, const TcTables &t, int images,
                             cudaStream_t s) {
-    if (n == 1024) return launch_tc5_lines_1024(rows, a, t, images, s);
+    if (n == 1024 || n == 4096) return launch_tc5_lines(n, rows, a, t, images, s);
     if (n == 4096) return rows ? tc_launch<64, true>(a, t, images, s) : tc_launch<64, false>(a, t, images, s);
     return cudaErrorInvalidValue;
 }

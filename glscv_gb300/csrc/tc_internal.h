@@ -15,9 +15,9 @@ struct TcTables {
     __half *f32_hi = nullptr, *f32_lo = nullptr;  // N1 = 32 (N = 1024)
     __half *f64_hi = nullptr, *f64_lo = nullptr;  // N1 = 64 (N = 4096)
     float2 *tw1024 = nullptr, *tw4096 = nullptr;
-    // the 32-point DFT as the tcgen05 B operand: FP16 hi (8 KB) then lo
-    // (8 KB), 128-byte-swizzled K-major image (tc5_fft.cu)
-    unsigned char *dft32_sw = nullptr;
+    // the 32- and 64-point DFTs as tcgen05 B operands: FP16 hi then lo,
+    // 128-byte-swizzled K-major images (tc5_fft.cu; 16 KB and 48 KB)
+    unsigned char *dft32_sw = nullptr, *dft64_sw = nullptr;
     void *block = nullptr;  // one allocation holding all of the above
 };
 
@@ -28,12 +28,12 @@ void tc_tables_destroy(TcTables *t);
 cudaError_t launch_tc_lines(int n, bool rows, const PassArgs &a, const TcTables &t, int images,
                             cudaStream_t s);
 
-// 1024-point lines on tcgen05 (tc5_fft.cu); the line count must be a
-// multiple of 4.
-cudaError_t launch_tc5_lines_1024(bool rows, const PassArgs &a, const TcTables &t, int images,
-                                  cudaStream_t s);
-// Host: the 32-point DFT B operand image (16 KB) from cos_sin[m] =
-// {cos, sin}(2 pi m / 32).
-void tc5_dft32_image(const double (*cos_sin)[2], unsigned char *dst16k);
+// 1024- or 4096-point lines on tcgen05 (tc5_fft.cu); the line count must
+// be a multiple of 4 resp. 2.
+cudaError_t launch_tc5_lines(int n, bool rows, const PassArgs &a, const TcTables &t, int images,
+                             cudaStream_t s);
+// Host: the N1-point DFT B operand image (N1 = 32: 16 KB, 64: 48 KB) from
+// cos_sin[m] = {cos, sin}(2 pi m / N1).
+void tc5_dft_image(int n1, const double (*cos_sin)[2], unsigned char *dst);
 
 }  // namespace glsfft
