@@ -57,37 +57,27 @@ static float2 twiddle(long long k, long long n) {
 
 // ---------------------------------------------- tensor-core form tables
 int glsfft::tc_tables_create(TcTables *t) {
-    const size_t f32_halves = 64 * 72, f64_halves = 128 * 136;  // 2N1 x (2N1 + 8)
-    const size_t dft_off = (2 * (f32_halves + f64_halves) * sizeof(__half) +
-                            (1024 + 4096) * sizeof(float2) + 16 + 1023) / 1024 * 1024;
+    // stage-B twiddles (1024 + 4096 complex), then the two DFT operand images
+    // at 1024-byte offsets
+    const size_t dft_off = ((1024 + 4096) * sizeof(float2) + 1023) / 1024 * 1024;
     const size_t dft64_off = dft_off + 16384;
-    const size_t bytes = dft64_off + 49152 + 1024;
+    const size_t bytes = dft64_off + 49152;
     std::vector<unsigned char> host(bytes, 0);
     unsigned char *p = host.data();
-    __half *h32 = reinterpret_cast<__half *>(p), *l32 = h32 + f32_halves;
-    __half *h64 = l32 + f32_halves, *l64 = h64 + f64_halves;
-    float2 *tw1 = reinterpret_cast<float2 *>(
-        (reinterpret_cast<uintptr_t>(l64 + f64_halves) + 15) & ~uintptr_t(15));
+    float2 *tw1 = reinterpret_cast<float2 *>(p);
     float2 *tw4 = tw1 + 1024;
-    auto fill = [](__half *hi, __half *lo, int n1) {
-        const int stride = 2 * n1 + 8;
-        for (int r = 0; r < 2 * n1; r++)
-            for (int c = 0; c < 2 * n1; c++) {
-                double re, im;  // F[k][n] = e^{-2 pi i k n / n1}
-                twiddle_d((long long)(r % n1) * (c % n1), n1, re, im);
-                // [Fr -Fi; Fi Fr]
-                const double v = (r < n1) == (c < n1) ? re : (r < n1 ? -im : im);
-                const __half h = __double2half(v);
-                hi[r * stride + c] = h;
-                lo[r * stride + c] = __double2half(v - (double)__half2float(h));
-            }
-    };
-    fill(h32, l32, 32);
-    fill(h64, l64, 64);
+    // w^(k1 n2) / N1: the four-step twiddle with the stage-C scale folded in
+    // (a power of two, so the division is exact)
     for (int k1 = 0; k1 < 32; k1++)
-        for (int n2 = 0; n2 < 32; n2++) tw1[k1 * 32 + n2] = twiddle((long long)k1 * n2, 1024);
+        for (int n2 = 0; n2 < 32; n2++) {
+            const float2 w = twiddle((long long)k1 * n2, 1024);
+            tw1[k1 * 32 + n2] = make_float2(w.x / 32.0f, w.y / 32.0f);
+        }
     for (int k1 = 0; k1 < 64; k1++)
-        for (int n2 = 0; n2 < 64; n2++) tw4[k1 * 64 + n2] = twiddle((long long)k1 * n2, 4096);
+        for (int n2 = 0; n2 < 64; n2++) {
+            const float2 w = twiddle((long long)k1 * n2, 4096);
+            tw4[k1 * 64 + n2] = make_float2(w.x / 64.0f, w.y / 64.0f);
+        }
     double cs[64][2];
     for (int n1 = 32; n1 <= 64; n1 *= 2) {
         for (int m = 0; m < n1; m++) {
@@ -107,14 +97,9 @@ int glsfft::tc_tables_create(TcTables *t) {
         return cuda_status(e);
     }
     unsigned char *b = static_cast<unsigned char *>(d);
-    auto rebase = [&](const void *hp) { return b + (static_cast<const unsigned char *>(hp) - p); };
     t->block = d;
-    t->f32_hi = reinterpret_cast<__half *>(rebase(h32));
-    t->f32_lo = reinterpret_cast<__half *>(rebase(l32));
-    t->f64_hi = reinterpret_cast<__half *>(rebase(h64));
-    t->f64_lo = reinterpret_cast<__half *>(rebase(l64));
-    t->tw1024 = reinterpret_cast<float2 *>(rebase(tw1));
-    t->tw4096 = reinterpret_cast<float2 *>(rebase(tw4));
+    t->tw1024 = reinterpret_cast<float2 *>(b);
+    t->tw4096 = reinterpret_cast<float2 *>(b) + 1024;
     t->dft32_sw = b + dft_off;
     t->dft64_sw = b + dft64_off;
     return GLSFFT_SUCCESS;
@@ -456,6 +441,7 @@ int glsfft_fft2d_tc(glsfft_context ctx, const void *src, void *dst, int count, i
     a.scale = scale ? 1.0f / (float)cols : 1.0f;
     a.flags = (inv ? PF_CONJ_IN : 0u) | (shift ? PF_SHIFT_COLS : 0u);
     a.in_img_bytes = a.out_img_bytes = bytes;
+    a.err = ctx->d_status;  // bounded waits record GLSFFT_ERROR_TIMEOUT here
     cudaError_t e = launch_tc_lines(cols, true, a, ctx->tc, count, s);
     if (e != cudaSuccess) return cuda_status(e);
     PassArgs b{};
@@ -466,6 +452,7 @@ int glsfft_fft2d_tc(glsfft_context ctx, const void *src, void *dst, int count, i
     b.scale = scale ? 1.0f / (float)rows : 1.0f;
     b.flags = (inv ? PF_CONJ_OUT : 0u) | (shift ? PF_SHIFT_ROWS : 0u);
     b.in_img_bytes = b.out_img_bytes = bytes;
+    b.err = ctx->d_status;
     return cuda_status(launch_tc_lines(rows, false, b, ctx->tc, count, s));
 }
 

@@ -63,9 +63,9 @@ struct PassArgs {
     // leaves its first tile's copy unissued and waits this many nanoseconds
     // for it, so the wait runs out
     long long stall_ns;
-    // launch with programmatic dependent launch (the row, column and POC
-    // column kernels; the streamed pass ignores it): the grid may become
-    // resident before its stream predecessor ends
+    // launch with programmatic dependent launch (every pass kernel begins
+    // with griddepcontrol.wait): the grid may become resident before its
+    // stream predecessor ends
     int pdl;
 };
 
