@@ -310,7 +310,8 @@ def shifted_frame_gpu(torch, base, sx: float, sy: float, noise, n: int):
     return hb
 
 
-def serving_sweep(g, ctx, torch, requests: int = 2000, repeats: int = 3, slots: int = 16) -> dict:
+def serving_sweep(g, ctx, torch, requests: int = 2000, repeats: int = 3, slots: int = 16,
+                  modes=("copy", "direct")) -> dict:
     """Config 5: Poisson arrivals (seed 5) of CV_32FC1 frame pairs sized 512^2,
     1024^2 or 2048^2 (mix .5/.35/.15) against 32 resident reference spectra
     (16 / 11 / 5 distinct smooth fields); every reference has 4 distinct
@@ -320,7 +321,10 @@ def serving_sweep(g, ctx, torch, requests: int = 2000, repeats: int = 3, slots: 
     the whole sweep `repeats` times; latency = scheduled arrival to result on
     the host, measured natively by the server, with each request's time
     split into arrival-thread lateness, queueing, issuing and device work plus
-    completion polling, and the device time between CUDA events."""
+    completion polling, and the device time between CUDA events.  Each frame
+    read mode of the server runs the whole sweep: "copy" (a copy-engine
+    transfer of the frame, the default) and "direct" (the row kernel reads
+    the page-locked host frame itself)."""
     import numpy as np
     from glscv_gb300 import workloads as wl
 
@@ -355,13 +359,28 @@ def serving_sweep(g, ctx, torch, requests: int = 2000, repeats: int = 3, slots: 
                          "estimator's own bias on sub-pixel shifts (the reference algorithm); "
                          "deviation vs the same frame served alone is the continuous-batching "
                          "check (0 = identical)",
-           "rates": []}
-    # every frame served alone (one request in flight): the reference result
-    # for the continuous-batching check; also loads every kernel
+           "modes": {}}
+    # every frame served alone (one request in flight, copy mode): the
+    # reference result for the continuous-batching check; also loads every
+    # kernel
     alone = {}
     for i, (n, rid, hb, _) in enumerate(frames):
         for _ in range(2):
             alone[i] = srv.wait(srv.submit(rid, hb.data_ptr()))[0]
+    for mode in modes:
+        srv.set_frame_read(mode == "direct")
+        out["modes"][mode] = {"rates": _serving_rates(srv, frames, by_size, alone, rng, requests,
+                                                      repeats)}
+    srv.set_frame_read(False)
+    out["stats"] = srv.stats()
+    srv.close()
+    del keep, frames
+    torch.cuda.empty_cache()
+    return out
+
+
+def _serving_rates(srv, frames, by_size, alone, rng, requests, repeats):
+    import numpy as np
     per_rate = {rate: [] for rate in SERVE_RATES}
     for rep in range(repeats):
         for rate in SERVE_RATES:
@@ -398,9 +417,10 @@ def serving_sweep(g, ctx, torch, requests: int = 2000, repeats: int = 3, slots: 
                                            [round(float(v), 4) for v in ph[tail].mean(axis=0)])),
                 "max_error_vs_true_shift_px": round(float(err), 4),
                 "max_dev_vs_alone_px": float(dev)})
+    rates = []
     for rate in SERVE_RATES:
         runs = per_rate[rate]
-        out["rates"].append({
+        rates.append({
             "offered_per_s": rate, "requests": requests,
             "pairs_per_s": [r["pairs_per_s"] for r in runs],
             "p50_ms": [r["p50_ms"] for r in runs],
@@ -413,20 +433,16 @@ def serving_sweep(g, ctx, torch, requests: int = 2000, repeats: int = 3, slots: 
             "tail_phases_ms": [r["tail_phases_ms"] for r in runs],
             "max_error_vs_true_shift_px": max(r["max_error_vs_true_shift_px"] for r in runs),
             "max_dev_vs_alone_px": max(r["max_dev_vs_alone_px"] for r in runs)})
-    out["stats"] = srv.stats()
-    srv.close()
-    del keep, frames
-    torch.cuda.empty_cache()
-    return out
+    return rates
 
 
-def serving_p99_1024(serving: dict | None):
+def serving_p99_1024(serving: dict | None, mode: str = "copy"):
     """The worst 1024^2 p99 over the repeats at the highest offered rate whose
     throughput kept up with the offer (within 5%), and that rate."""
-    if not serving:
+    if not serving or mode not in serving["modes"]:
         return None, None
     best = None
-    for r in serving["rates"]:
+    for r in serving["modes"][mode]["rates"]:
         if min(r["pairs_per_s"]) >= 0.95 * r["offered_per_s"]:
             best = r
     if best is None:
@@ -1027,7 +1043,8 @@ def run_own(args) -> None:
         cpu_more = cpu_detail()
         serving = None if args.no_serving else serving_sweep(g, ctx, torch,
                                                              slots=args.serve_slots)
-        serve_p99, serve_rate = serving_p99_1024(serving)
+        serve_p99, serve_rate = serving_p99_1024(serving, "copy")
+        serve_p99_direct, serve_rate_direct = serving_p99_1024(serving, "direct")
         precision = precision_form(ctx, torch, s)
         uneven = None if args.no_uneven else uneven_batch(g, ctx, torch, s, args.no_autotune)
         spectrum = spectrum_ops(ctx, torch, s)
@@ -1045,6 +1062,8 @@ def run_own(args) -> None:
             # the other parts of the metric, at the top level
             "pc_p99_ms": pc["p99_ms"] if pc else None,
             "serving_p99_ms_1024": serve_p99,
+            "serving_direct_p99_ms_1024": serve_p99_direct,
+            "serving_direct_p99_rate_per_s": serve_rate_direct,
             "serving_p99_rate_per_s": serve_rate,
             "tc_over_fp32": {c["shape"]: c["tc_over_fp32_time"] for c in precision["cases"]},
             "plain_per_image": {"value": round(plain_value, 3), "unit": UNIT,

@@ -99,6 +99,7 @@ _SIGNATURES = {
                                    _dp, _dp]),
     "glsfft_server_replay_traced": (_ip, [_vp, _ip, _dp, ctypes.POINTER(_ip), ctypes.POINTER(_vp),
                                           _ip, _dp, _dp, _dp]),
+    "glsfft_server_set_frame_read": (_ip, [_vp, _ip]),
     "glsfft_server_stats": (_ip, [_vp, ctypes.POINTER(ctypes.c_longlong)]),
     "glsfft_server_destroy": (_ip, [_vp]),
 }
@@ -458,6 +459,12 @@ class Server:
         if phases:
             return out + ([list(ph[6 * k:6 * k + 6]) for k in range(n)],)
         return out
+
+    def set_frame_read(self, direct: bool) -> None:
+        """True: the row kernel reads page-locked host frames itself (no
+        copy-engine transfer); False: the default copy."""
+        check(lib().glsfft_server_set_frame_read(self.handle, int(bool(direct))),
+              "server_set_frame_read")
 
     def stats(self) -> dict:
         out = (ctypes.c_longlong * 8)()

@@ -52,6 +52,7 @@ enum { REQ_QUEUED = 0, REQ_RUNNING = 1, REQ_DONE = 2, REQ_FAILED = 3 };
 struct Request {
     int ref = 0;
     const float *frame = nullptr;  // host pointer, valid until completion
+    bool direct = false;           // the row kernel reads `frame` itself
     int box = 5;
     // arrival: the scheduled arrival (latency counts from it); submitted: when
     // the request was queued; admitted: when a dispatcher took a slot and
@@ -101,6 +102,7 @@ struct glsfft_server_s {
     std::unordered_map<long long, Request> reqs;
     long long next_ticket = 1;
     int in_flight = 0;
+    bool direct_read = false;  // glsfft_server_set_frame_read
     bool stop = false;
     std::vector<std::thread> dispatchers;
     std::thread poller;
@@ -130,11 +132,15 @@ int launch_request(glsfft_server srv, const Reference &ref, const Request &rq, S
     // zeroes the argmax key; the last block of the inverse row pass computes
     // the centroid and writes it into the slot's mapped pinned buffer), the event
     cudaError_t e = cudaEventRecord(slot.start, s);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(frame, rq.frame, 4 * n, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess && !rq.direct)
+        e = cudaMemcpyAsync(frame, rq.frame, 4 * n, cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = cudaEventRecord(slot.copied, s);
     if (e != cudaSuccess) return cuda_status(e);
     PassArgs a{};
-    a.in0 = frame;
+    // direct: the windowed row pass loads the page-locked host frame over the
+    // host link itself (its device address is the host address under unified
+    // addressing), so no copy-engine transfer precedes it
+    a.in0 = rq.direct ? rq.frame : frame;
     a.out0 = f2;
     a.window = win;
     a.rows = rows;
@@ -296,12 +302,25 @@ void poller_main(glsfft_server srv) {
     }
 }
 
-long long submit_locked(glsfft_server srv, int ref_id, const float *frame, int box,
+// Whether a kernel on the server's device may read `frame` directly: page-
+// locked host memory whose device address is its host address.
+bool frame_readable(glsfft_server srv, const float *frame) {
+    cudaPointerAttributes at{};
+    if (cudaPointerGetAttributes(&at, frame) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    (void)srv;
+    return at.type == cudaMemoryTypeHost && at.devicePointer == frame;
+}
+
+long long submit_locked(glsfft_server srv, int ref_id, const float *frame, bool direct, int box,
                         Clock::time_point arrival) {
     const long long ticket = srv->next_ticket++;
     Request rq;
     rq.ref = ref_id;
     rq.frame = frame;
+    rq.direct = direct;
     rq.box = box;
     rq.arrival = arrival;
     rq.submitted = Clock::now();
@@ -446,11 +465,12 @@ int glsfft_server_add_reference(glsfft_server srv, const float *frame, const flo
 int glsfft_server_submit(glsfft_server srv, int ref_id, const float *host_frame, int box,
                          long long *ticket) {
     if (!srv || !host_frame || !ticket || box < 1) return GLSFFT_ERROR_INVALID_VALUE;
+    const bool direct = srv->direct_read && frame_readable(srv, host_frame);
     std::lock_guard<std::mutex> lock(srv->mu);
     if (ref_id < 0 || ref_id >= (int)srv->refs.size()) return GLSFFT_ERROR_INVALID_VALUE;
     const Reference &ref = srv->refs[ref_id];
     if (workspace_bytes(ref.rows, ref.cols) > srv->arena.capacity()) return GLSFFT_ERROR_BUDGET;
-    *ticket = submit_locked(srv, ref_id, host_frame, box, Clock::now());
+    *ticket = submit_locked(srv, ref_id, host_frame, direct, box, Clock::now());
     srv->cv_dispatch.notify_one();
     return GLSFFT_SUCCESS;
 }
@@ -481,6 +501,9 @@ int glsfft_server_replay_traced(glsfft_server srv, int n, const double *offsets_
         }
     }
     std::vector<long long> tickets(n);
+    std::vector<char> direct(n, 0);
+    if (srv->direct_read)
+        for (int k = 0; k < n; k++) direct[k] = frame_readable(srv, host_frames[k]);
     const Clock::time_point t0 = Clock::now();
     for (int k = 0; k < n; k++) {
         // open-loop arrivals: latency counts from the scheduled arrival time.
@@ -495,7 +518,7 @@ int glsfft_server_replay_traced(glsfft_server srv, int n, const double *offsets_
                 std::this_thread::sleep_for(left - std::chrono::microseconds(250));
         }
         std::lock_guard<std::mutex> lock(srv->mu);
-        tickets[k] = submit_locked(srv, ref_ids[k], host_frames[k], box, at);
+        tickets[k] = submit_locked(srv, ref_ids[k], host_frames[k], direct[k] != 0, box, at);
         srv->cv_dispatch.notify_one();
     }
     int status = GLSFFT_SUCCESS;
@@ -524,6 +547,13 @@ int glsfft_server_replay(glsfft_server srv, int n, const double *offsets_s, cons
                          double *results5) {
     return glsfft_server_replay_traced(srv, n, offsets_s, ref_ids, host_frames, box, latencies_s,
                                        results5, nullptr);
+}
+
+int glsfft_server_set_frame_read(glsfft_server srv, int direct) {
+    if (!srv || (direct != 0 && direct != 1)) return GLSFFT_ERROR_INVALID_VALUE;
+    std::lock_guard<std::mutex> lock(srv->mu);
+    srv->direct_read = direct != 0;
+    return GLSFFT_SUCCESS;
 }
 
 int glsfft_server_stats(glsfft_server srv, long long *out8) {

@@ -535,6 +535,16 @@ GLSFFT_API int glsfft_server_replay_traced(glsfft_server server, int n, const do
                                            int box, double *latencies_s, double *results5,
                                            double *phases6);
 
+/*
+ * How requests bring their frame to the device (no reference counterpart).
+ * 0 (the default): a copy-engine transfer into the request's workspace,
+ * then the row pass.  1: the windowed row pass reads the frame from host
+ * memory itself, for frames in page-locked memory (cudaHostAlloc /
+ * cudaHostRegister; other frames keep the copy).  Applies to requests
+ * submitted afterwards.
+ */
+GLSFFT_API int glsfft_server_set_frame_read(glsfft_server server, int direct);
+
 /* Counters: admitted, completed, failed, peak in flight, peak queue length,
  * budget bytes, peak budget bytes in use, resident references. */
 GLSFFT_API int glsfft_server_stats(glsfft_server server, long long *out8);

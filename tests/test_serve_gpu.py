@@ -121,3 +121,23 @@ def test_submit_errors_and_destroy_with_queue(ctx, torch_cuda):
     for _ in range(50):
         srv.submit(frames[0][0], frames[0][1].data_ptr())
     srv.close()  # drops the queue, finishes the running requests, returns
+
+
+def test_direct_frame_read_equals_copy(ctx, torch_cuda):
+    """glsfft_server_set_frame_read(1): the row kernel reads page-locked host
+    frames itself.  Results are bit-identical to the copy mode, alone and in
+    a mix; a pageable frame falls back to the copy and gives the same result."""
+    torch = torch_cuda
+    with g.Server(ctx, slots=8, hbm_budget=1 << 30) as srv:
+        refs, frames, keep = _setup(torch, srv, [256, 1024, 2048], seed=50)
+        copy = [srv.wait(srv.submit(rid, hb.data_ptr()))[0] for rid, hb, *_ in frames]
+        srv.set_frame_read(True)
+        direct = [srv.wait(srv.submit(rid, hb.data_ptr()))[0] for rid, hb, *_ in frames]
+        assert direct == copy
+        tickets = [srv.submit(frames[i][0], frames[i][1].data_ptr()) for i in [0, 5, 2, 8, 1, 4] * 3]
+        mixed = [srv.wait(t)[0] for t in tickets]
+        assert mixed == [copy[i] for i in [0, 5, 2, 8, 1, 4] * 3]
+        pageable = np.ascontiguousarray(frames[3][4])
+        r = srv.wait(srv.submit(frames[3][0], pageable.ctypes.data))[0]
+        assert r == copy[3]
+        srv.set_frame_read(False)
