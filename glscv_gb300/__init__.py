@@ -461,8 +461,8 @@ class Server:
         return out
 
     def set_frame_read(self, direct: bool) -> None:
-        """True: the row kernel reads page-locked host frames itself (no
-        copy-engine transfer); False: the default copy."""
+        """True (the default): the row kernel reads page-locked host frames
+        itself (no copy-engine transfer); False: a copy-engine transfer."""
         check(lib().glsfft_server_set_frame_read(self.handle, int(bool(direct))),
               "server_set_frame_read")
 

@@ -102,7 +102,7 @@ struct glsfft_server_s {
     std::unordered_map<long long, Request> reqs;
     long long next_ticket = 1;
     int in_flight = 0;
-    bool direct_read = false;  // glsfft_server_set_frame_read
+    bool direct_read = true;  // glsfft_server_set_frame_read
     bool stop = false;
     std::vector<std::thread> dispatchers;
     std::thread poller;

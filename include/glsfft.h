@@ -537,10 +537,13 @@ GLSFFT_API int glsfft_server_replay_traced(glsfft_server server, int n, const do
 
 /*
  * How requests bring their frame to the device (no reference counterpart).
- * 0 (the default): a copy-engine transfer into the request's workspace,
- * then the row pass.  1: the windowed row pass reads the frame from host
- * memory itself, for frames in page-locked memory (cudaHostAlloc /
- * cudaHostRegister; other frames keep the copy).  Applies to requests
+ * 1 (the default): the windowed row pass reads the frame from host memory
+ * itself, for frames in page-locked memory (cudaHostAlloc /
+ * cudaHostRegister; other frames are copied).  0: a copy-engine transfer
+ * into the request's workspace, then the row pass.  On GB300 the copy path
+ * showed H2D tails of several milliseconds under load with many distinct
+ * frames, the direct read did not; the copy path sustains more pairs per
+ * second at saturation.  Results are identical.  Applies to requests
  * submitted afterwards.
  */
 GLSFFT_API int glsfft_server_set_frame_read(glsfft_server server, int direct);

@@ -124,12 +124,14 @@ def test_submit_errors_and_destroy_with_queue(ctx, torch_cuda):
 
 
 def test_direct_frame_read_equals_copy(ctx, torch_cuda):
-    """glsfft_server_set_frame_read(1): the row kernel reads page-locked host
-    frames itself.  Results are bit-identical to the copy mode, alone and in
-    a mix; a pageable frame falls back to the copy and gives the same result."""
+    """glsfft_server_set_frame_read: 1 (the default) has the row kernel read
+    page-locked host frames itself, 0 copies them first.  Results are
+    bit-identical, alone and in a mix; a pageable frame falls back to the
+    copy and gives the same result."""
     torch = torch_cuda
     with g.Server(ctx, slots=8, hbm_budget=1 << 30) as srv:
         refs, frames, keep = _setup(torch, srv, [256, 1024, 2048], seed=50)
+        srv.set_frame_read(False)
         copy = [srv.wait(srv.submit(rid, hb.data_ptr()))[0] for rid, hb, *_ in frames]
         srv.set_frame_read(True)
         direct = [srv.wait(srv.submit(rid, hb.data_ptr()))[0] for rid, hb, *_ in frames]
@@ -140,4 +142,3 @@ def test_direct_frame_read_equals_copy(ctx, torch_cuda):
         pageable = np.ascontiguousarray(frames[3][4])
         r = srv.wait(srv.submit(frames[3][0], pageable.ctypes.data))[0]
         assert r == copy[3]
-        srv.set_frame_read(False)
