@@ -69,8 +69,8 @@ def parse():
                    help="run phaseCorrelate (Hann window) on one NxN pair three times and exit "
                         "(for ncu)")
     p.add_argument("--profile-tc", type=int, default=0, metavar="N",
-                   help="run the precision form (split-FP16 tensor-core FFT) forward on one NxN "
-                        "image three times and exit (for ncu)")
+                   help="run the precision form (split-FP16 tensor-core FFT) forward on --images "
+                        "NxN images three times and exit (for ncu)")
     p.add_argument("--profile-fft", type=int, default=0, metavar="N",
                    help="run gls::fft forward on one NxN image three times with the size's "
                         "default pass schedules and exit (for ncu)")
@@ -879,14 +879,15 @@ def run_own(args) -> None:
         return
 
     if args.profile_tc:
-        # the precision form on one image: three forward transforms, for ncu
-        n = args.profile_tc
-        x = torch.from_numpy(wl.complex_uniform(n, n, 4)).cuda()
+        # the precision form on --images images: three forward transforms, for ncu
+        n, count = args.profile_tc, args.images
+        x = torch.from_numpy(np.stack([wl.complex_uniform(n, n, 4)] * count)).cuda()
         y = torch.empty_like(x)
         for _ in range(3):
-            ctx.fft2d_tc(x.data_ptr(), y.data_ptr(), 1, n, n, 0, s)
+            ctx.fft2d_tc(x.data_ptr(), y.data_ptr(), count, n, n, 0, s)
         torch.cuda.synchronize()
-        print(json.dumps({"profile_tc": n}), flush=True)
+        print(json.dumps({"profile_tc": n, "images": count, "device_status": ctx.device_status()}),
+              flush=True)
         ctx.close()
         return
 
