@@ -177,18 +177,86 @@ __device__ __forceinline__ double poc_sum(const float *surface, int cols, const 
         }
     return acc;
 }
+
+// The three sums at once on one warp, exactly, when no rounding can occur:
+// every term x*v, y*v, v of a finite float v and an integer coordinate below
+// 2^13 is m * 2^e with an integer m of at most 37 bits; if, for each sum, the
+// largest term's leading bit and the smallest term's lowest bit are at most
+// 46 binades apart, every partial sum of up to 32 terms is a multiple of the
+// lowest bit below 2^53 of it, so the reference's sequential FP64 sum never
+// rounds and equals the exact integer sum -- which one warp forms in any
+// order (64-bit integers, shuffles) and converts once.  Returns false (on
+// every lane) when the box has more than 32 values, a non-finite value, or a
+// wider range; the caller then runs the sequential FP64 sums.  GB300's FP64
+// pipe makes the sequential chain of 25 dependent additions cost microseconds.
+__device__ __forceinline__ bool poc_sums_exact(const float *vals, const PocBox &b, double *out3) {
+    const int lane = threadIdx.x & 31;
+    const int w = b.maxc - b.minc + 1, n = w * (b.maxr - b.minr + 1);
+    if (n > 32) return false;
+    unsigned long long mv = 0;  // significand of v
+    int e = 0;                  // v = +-mv * 2^e
+    bool neg = false, ok = true;
+    unsigned cx = 0, cy = 0;
+    if (lane < n) {
+        const unsigned bits = __float_as_uint(vals[lane]);
+        const int e8 = (int)((bits >> 23) & 0xFF);
+        ok = e8 != 0xFF;
+        neg = bits >> 31;
+        mv = (bits & 0x7FFFFFu) | (e8 ? 0x800000u : 0u);
+        e = e8 ? e8 - 150 : -149;
+        cx = (unsigned)(b.minc + lane % w);
+        cy = (unsigned)(b.minr + lane / w);
+    }
+    if (!__all_sync(0xffffffffu, ok)) return false;
+    long long q[3];
+    int lo[3];
+#pragma unroll
+    for (int which = 0; which < 3; which++) {
+        const unsigned long long m = mv * (which == 0 ? cx : which == 1 ? cy : 1u);
+        int top = m ? e + (63 - __clzll((long long)m)) : -100000;
+        int low = m ? e : 100000;
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            top = max(top, __shfl_xor_sync(0xffffffffu, top, off));
+            low = min(low, __shfl_xor_sync(0xffffffffu, low, off));
+        }
+        if (low == 100000) {  // every term is zero: the sum is +0
+            q[which] = 0;
+            lo[which] = 0;
+            continue;
+        }
+        if (top - low > 46) return false;
+        const long long t = m ? (long long)(m << (e - low)) : 0;
+        q[which] = neg ? -t : t;
+        lo[which] = low;
+    }
+#pragma unroll
+    for (int which = 0; which < 3; which++) {
+        long long sum = q[which];
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, off);
+        // |sum| < 2^53: exact as a double; times the power of two 2^lo, exact
+        const double p2 = __longlong_as_double((long long)(lo[which] + 1023) << 52);
+        if (lane == 0) out3[which] = sum == 0 ? 0.0 : __dmul_rn((double)sum, p2);
+    }
+    return true;
+}
 // The result from the three sums: response = sum / (rows*cols)
 // (:224-225), then sum + DBL_EPSILON divides (:128), shift = center -
 // centroid (:228-230).
+// part < 0: all of it on this thread; part 0 / 1 / 2: only dx / dy / the
+// response, peak index and peak value (three threads of different warps run
+// the two FP64 divisions side by side).
 __device__ __forceinline__ void poc_result(int rows, int cols, const PocBox &b, double sx,
-                                           double sy, double sum, double *res) {
-    const double response = sum / ((double)rows * (double)cols);
+                                           double sy, double sum, double *res, int part = -1) {
+    if (part < 0 || part == 2) {
+        res[2] = sum / ((double)rows * (double)cols);
+        res[3] = (double)(b.py * cols + b.px);
+        res[4] = b.peak;
+    }
     sum = __dadd_rn(sum, 2.220446049250313e-16);  // DBL_EPSILON, glsPhaseCorrelate.cpp:128
-    res[0] = __dsub_rn((double)cols / 2.0, sx / sum);
-    res[1] = __dsub_rn((double)rows / 2.0, sy / sum);
-    res[2] = response;
-    res[3] = (double)(b.py * cols + b.px);
-    res[4] = b.peak;
+    if (part < 0 || part == 0) res[0] = __dsub_rn((double)cols / 2.0, sx / sum);
+    if (part < 0 || part == 1) res[1] = __dsub_rn((double)rows / 2.0, sy / sum);
 }
 // boxes up to this many values are read into shared memory by the whole
 // block at once (independent L2 reads in flight) before thread 0 sums them
@@ -281,18 +349,26 @@ __global__ void __launch_bounds__(LINES *LineFft<N, E>::T)
                         for (int i = threadIdx.x; i < n; i += blockDim.x)
                             s_box[i] = __ldcg(surf + (size_t)(b.minr + i / w) * N + b.minc + i % w);
                     __syncthreads();
-                    // the three FP64 sums on lane 0 of three warps (separate
-                    // SM partitions), then thread 0 forms the result (a result
-                    // in mapped host memory needs no system fence: the host
-                    // reads it after synchronising with the kernel)
+                    // the three FP64 sums: exactly on warp 0 when no rounding
+                    // can occur, else sequentially on lane 0 of three warps
+                    // (separate SM partitions); then thread 0 forms the result
+                    // (a result in mapped host memory needs no system fence:
+                    // the host reads it after synchronising with the kernel)
                     __shared__ double s_sum[3];
+                    __shared__ int s_exact;
                     const int warp = threadIdx.x >> 5, warps = (blockDim.x + 31) >> 5;
-                    if ((threadIdx.x & 31) == 0)
+                    if (warp == 0) {
+                        const bool ex = staged && poc_sums_exact(s_box, b, s_sum);
+                        if (threadIdx.x == 0) s_exact = ex;
+                    }
+                    __syncthreads();
+                    if (!s_exact && (threadIdx.x & 31) == 0)
                         for (int which = warp; which < 3; which += warps)
                             s_sum[which] = poc_sum(surf, N, b, staged ? s_box : nullptr, which);
                     __syncthreads();
-                    if (threadIdx.x == 0)
-                        poc_result(a.rows, N, b, s_sum[0], s_sum[1], s_sum[2], a.result);
+                    if ((threadIdx.x & 31) == 0 && (warps >= 3 ? warp < 3 : warp == 0))
+                        poc_result(a.rows, N, b, s_sum[0], s_sum[1], s_sum[2], a.result,
+                                   warps >= 3 ? warp : -1);
                 }
             }
         }
