@@ -79,6 +79,7 @@ _SIGNATURES = {
     "glsfft_batch_status": (_ip, [_vp, _vp]),
     "glsfft_batch_info": (_ip, [_vp, ctypes.POINTER(_ip), ctypes.POINTER(_ip),
                                 ctypes.POINTER(_ip)]),
+    "glsfft_batch_workspace": (_ip, [_vp, ctypes.POINTER(_ip), ctypes.POINTER(_sz)]),
     "glsfft_batch_inject_stall": (_ip, [_vp, ctypes.c_longlong]),
     "glsfft_batch_get_schedule": (_ip, [_vp, ctypes.POINTER(_ip)]),
     "glsfft_batch_tuning": (_ip, [_vp, _ip, ctypes.POINTER(_ip), _dp, ctypes.POINTER(_ip)]),
@@ -349,6 +350,14 @@ class Batch:
         check(lib().glsfft_batch_info(self.handle, ctypes.byref(a), ctypes.byref(b),
                                       ctypes.byref(c)), "batch_info")
         return {"persistent_images": a.value, "items": b.value, "grid": c.value}
+
+    def workspace(self):
+        """glsfft_batch_workspace: images with a column-tiled workspace and
+        the bytes the plan holds for them."""
+        n, b = _ip(), _sz()
+        check(lib().glsfft_batch_workspace(self.handle, ctypes.byref(n), ctypes.byref(b)),
+              "batch_workspace")
+        return {"tiled_images": n.value, "bytes": b.value}
 
     def inject_stall(self, wait_limit_ns: int) -> None:
         check(lib().glsfft_batch_inject_stall(self.handle, int(wait_limit_ns)), "inject_stall")

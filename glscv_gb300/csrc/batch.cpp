@@ -33,6 +33,7 @@ struct glsfft_batch_s {
     int grid = 0;
     int variant = BATCH_TMA_WS3;   // the fastest variant measured on GB300
     void *d_mem = nullptr;  // tensor maps | images | passes | items | head, done, error
+    void *d_work = nullptr;  // the images' column-tiled workspaces (BatchImage::work)
     BatchArgs args{};
     std::vector<BatchImage> images;
     std::vector<BatchPass> passes;
@@ -203,6 +204,22 @@ int glsfft::make_column_tmap(void *tmap128, const void *img, int rows, int cols)
     return make_tmap_2d(tmap128, img, cols, rows, w, br);
 }
 
+int glsfft::make_tiled_tmap(void *tmap128, const void *work, int rows, int cols) {
+    if (!batch_tiled_ok(rows, cols)) return GLSFFT_ERROR_INVALID_VALUE;
+    auto enc = tmap_encoder();
+    if (!enc) return GLSFFT_ERROR_CUDA;
+    const int w = kBatchTileElems / rows, lines = kBatchTileElems / cols;
+    cuuint64_t dims[3] = {(cuuint64_t)w, (cuuint64_t)(cols / w), (cuuint64_t)rows};
+    cuuint64_t strides[2] = {(cuuint64_t)rows * w * sizeof(float2), (cuuint64_t)w * sizeof(float2)};
+    cuuint32_t box[3] = {(cuuint32_t)w, (cuuint32_t)(cols / w), (cuuint32_t)lines};
+    cuuint32_t estr[3] = {1, 1, 1};
+    CUresult r = enc(reinterpret_cast<CUtensorMap *>(tmap128), CU_TENSOR_MAP_DATA_TYPE_UINT64, 3,
+                     const_cast<void *>(work), dims, strides, box, estr,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                     CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS ? GLSFFT_SUCCESS : GLSFFT_ERROR_CUDA;
+}
+
 extern "C" {
 
 int glsfft_batch_create(glsfft_context ctx, int count, const void *const *srcs,
@@ -265,7 +282,7 @@ int glsfft_batch_create(glsfft_context ctx, int count, const void *const *srcs,
         if (!st) items = order_items(plan->images, plan->passes, plan->lag_items);
         plan->n_items = (int)items.size();
         const size_t ni = plan->images.size();
-        const size_t b_tm = 128 * ni;
+        const size_t b_tm = 128 * kBatchTmapsPerImage * ni;
         const size_t b_im = sizeof(BatchImage) * ni;
         const size_t b_ps = sizeof(BatchPass) * plan->passes.size();
         const size_t b_it = sizeof(BatchItem) * items.size();
@@ -279,11 +296,37 @@ int glsfft_batch_create(glsfft_context ctx, int count, const void *const *srcs,
             cudaGetLastError();
             st = GLSFFT_ERROR_OUT_OF_MEMORY;
         }
+        // Column-tiled workspaces (one image each, 256-byte aligned) for
+        // the images whose shape allows them, when they fit the context's
+        // budget next to the plan's tables; otherwise the columns passes
+        // read and write dst in place through the column map.
+        size_t b_work = 0;
+        for (const BatchImage &im : plan->images)
+            if (batch_tiled_ok(im.rows, im.cols))
+                b_work += up(sizeof(float2) * (size_t)im.rows * im.cols);
+        if (!st && b_work && (!ctx->budget || total + b_work <= ctx->budget) &&
+            cudaMalloc(&plan->d_work, b_work) != cudaSuccess) {
+            cudaGetLastError();
+            plan->d_work = nullptr;
+        }
+        if (plan->d_work) {
+            char *w = static_cast<char *>(plan->d_work);
+            for (BatchImage &im : plan->images) {
+                if (!batch_tiled_ok(im.rows, im.cols)) continue;
+                im.work = reinterpret_cast<float2 *>(w);
+                w += up(sizeof(float2) * (size_t)im.rows * im.cols);
+            }
+        }
         if (!st) {
             std::vector<unsigned char> host(o_st, 0);
-            for (size_t i = 0; i < ni && !st; i++)
-                st = make_column_tmap(host.data() + 128 * i, plan->images[i].dst,
-                                      plan->images[i].rows, plan->images[i].cols);
+            for (size_t i = 0; i < ni && !st; i++) {
+                BatchImage &im = plan->images[i];
+                unsigned char *tm = host.data() + 128 * kBatchTmapsPerImage * i;
+                st = make_column_tmap(tm, im.dst, im.rows, im.cols);
+                // an encoder that refuses the tiled map leaves the image in place
+                if (!st && im.work && make_tiled_tmap(tm + 128, im.work, im.rows, im.cols))
+                    im.work = nullptr;
+            }
             std::memcpy(host.data() + o_im, plan->images.data(), b_im);
             std::memcpy(host.data() + o_ps, plan->passes.data(), b_ps);
             std::memcpy(host.data() + o_it, items.data(), b_it);
@@ -313,6 +356,7 @@ int glsfft_batch_create(glsfft_context ctx, int count, const void *const *srcs,
         if (plan->exec) cudaGraphExecDestroy(plan->exec);
         if (plan->graph) cudaGraphDestroy(plan->graph);
         if (plan->d_mem) cudaFree(plan->d_mem);
+        if (plan->d_work) cudaFree(plan->d_work);
         delete plan;
         return st;
     }
@@ -385,6 +429,20 @@ int glsfft_batch_info(glsfft_batch plan, int *persistent_images, int *items, int
     if (persistent_images) *persistent_images = plan->n_images;
     if (items) *items = plan->n_items;
     if (grid) *grid = plan->grid;
+    return GLSFFT_SUCCESS;
+}
+
+int glsfft_batch_workspace(glsfft_batch plan, int *tiled_images, size_t *bytes) {
+    if (!plan) return GLSFFT_ERROR_INVALID_VALUE;
+    int n = 0;
+    size_t b = 0;
+    for (const BatchImage &im : plan->images) {
+        if (!im.work) continue;
+        n++;
+        b += (sizeof(float2) * (size_t)im.rows * im.cols + 255) / 256 * 256;
+    }
+    if (tiled_images) *tiled_images = n;
+    if (bytes) *bytes = b;
     return GLSFFT_SUCCESS;
 }
 
@@ -718,6 +776,7 @@ int glsfft_batch_destroy(glsfft_batch plan) {
     if (plan->exec) cudaGraphExecDestroy(plan->exec);
     if (plan->graph) cudaGraphDestroy(plan->graph);
     if (plan->d_mem) cudaFree(plan->d_mem);
+    if (plan->d_work) cudaFree(plan->d_work);
     delete plan;
     return GLSFFT_SUCCESS;
 }

@@ -12,12 +12,23 @@ constexpr int kBatchMaxPasses = 4;      // passes per image (2 transforms)
 
 // One image of a batch plan.  Pass 0 reads src; every later pass reads and
 // writes dst (in place), so src may equal dst.
+//
+// When `work` is set (the warp-specialised kernel; images with
+// 4096 <= rows * cols <= 2^20), a rows pass writes its result to `work` in
+// the column-tiled layout instead of to dst, and the columns pass that
+// follows reads its tile from there as one contiguous block and writes dst.
+// Column-tiled layout: with W = kBatchTileElems / rows columns per tile,
+// pixel (r, c) is at work[((c / W) * rows + r) * W + c % W] -- a columns
+// tile is rows * W consecutive pixels, and the W-wide pieces of one row are
+// rows * W apart.  Every pass then reads its tile with one contiguous copy
+// (rows from src or dst, columns from work), and no pass reads a buffer
+// that the same pass writes, so src may still equal dst.
 struct BatchImage {
     const float2 *src;
     float2 *dst;
+    float2 *work;              // column-tiled workspace, or null
     int rows, cols;
     int row_tiles, col_tiles;  // tiles of a rows pass / a columns pass
-    int pad0, pad1;
 };
 
 // One pass of the chain every image runs through.
@@ -48,7 +59,8 @@ struct BatchArgs {
     int *error;            // set to a non-zero code when a bounded wait expires
     const float2 *tw;      // twiddle tables (entries [n, 2n) for length n)
     long long wait_limit_ns;  // bound on one dependency wait
-    const void *tmaps;     // warp-specialised kernel: one 128-B CUtensorMap per image (dst)
+    const void *tmaps;     // warp-specialised kernel: two 128-B CUtensorMaps per image
+                           // (kBatchTmapsPerImage): the column map of dst, the tiled map of work
     int claim_chunk;       // warp-specialised kernel: items claimed per queue atomic (1..4)
     int claim_ahead;       // 1: claim the next chunk before working on the current one
     unsigned long long *stats;  // warp-specialised kernel: kBatchStats timing sums, or null
@@ -88,5 +100,24 @@ int batch_ws_grid(int device, int blocks_per_sm);
 // Build the 2-D tensor map (8-byte elements, box W x min(rows, 256)) that the
 // warp-specialised kernel uses to stage column tiles of `img` (rows x cols).
 int make_column_tmap(void *tmap128, const void *img, int rows, int cols);
+
+// Tensor maps per image in BatchArgs::tmaps: [0] the column map of dst,
+// [1] the tiled map of work (zeroed when the image has no workspace).
+constexpr int kBatchTmapsPerImage = 2;
+
+// Whether an image of this shape uses the column-tiled workspace: whole
+// tiles both ways and one rows tile = one tensor box (W, cols / W, lines),
+// every box dimension <= 256.
+__host__ __device__ constexpr bool batch_tiled_ok(int rows, int cols) {
+    return rows >= 16 && cols >= 16 && rows <= 1024 && (long long)rows * cols >= kBatchTileElems &&
+           (long long)rows * cols <= 256LL * kBatchTileElems;
+}
+
+// Build the 3-D tensor map through which a rows pass stores one tile into
+// the column-tiled layout of `work` (rows x cols): dimensions (W, cols / W,
+// rows) with strides (8, rows * W * 8, W * 8) bytes, box (W, cols / W,
+// kBatchTileElems / cols) -- the box lands in shared memory as the tile's
+// rows, one after another.
+int make_tiled_tmap(void *tmap128, const void *work, int rows, int cols);
 
 }  // namespace glsfft

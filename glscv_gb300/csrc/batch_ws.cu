@@ -7,15 +7,19 @@
 // Accelerator:
 //   * a rows tile (LINES contiguous rows) is one cp.async.bulk copy;
 //   * a columns tile (W adjacent columns x N rows, W*8 = 32..512 bytes per
-//     row) is read as 2-D boxes through a per-image tensor map
-//     (cp.async.bulk.tensor.2d) -- the column staging that replaces the
-//     reference's separate tiled/untiled copy passes (glsCV/glsCopy.cpp).
+//     row) is one cp.async.bulk copy of a contiguous block when the image
+//     has a column-tiled workspace (BatchImage::work; the rows pass before
+//     stored its tile there with one 3-D tensor box), else 2-D boxes through
+//     a per-image tensor map of dst (cp.async.bulk.tensor.2d) -- the column
+//     staging that replaces the reference's separate tiled/untiled copy
+//     passes (glsCV/glsCopy.cpp).
 // Completion of each copy lands on the stage's "full" mbarrier.  The compute
 // warps read their 16 values per thread from the stage, run the Stockham
 // passes (exchanging through the same buffer), write the results back into
 // the stage in the image's layout and arrive on the stage's "computed"
 // mbarrier.  The storer writes the tile out with the TMA (one cp.async.bulk
-// for a rows tile, 2-D tensor boxes for a columns tile), arrives on the
+// for a rows tile, or one 3-D tensor box into the workspace; 2-D tensor
+// boxes for a columns tile), arrives on the
 // stage's "empty" mbarrier as soon as the store has read the stage (the
 // loader then refills it), waits for the store's writes and publishes the
 // tile at once (release fence + counter), so dependent passes never wait on
@@ -43,10 +47,11 @@ constexpr size_t kStageBytes = kStageElems * sizeof(float2);
 
 struct StageInfo {
     float2 *dst;
+    float2 *work;  // the image's column-tiled workspace, or null
     int rows, cols, tile, image;
     int pass, along_rows, flags, scale;
     int valid;  // 0: no more work
-    int pad[5];
+    int pad[3];
 };
 
 template <int ST>
@@ -275,6 +280,7 @@ __global__ void __launch_bounds__(kBlock, MINB) fft_batch_ws(BatchArgs a) {
             }
             const BatchItem &it = *itp;
             inf.dst = im.dst;
+            inf.work = im.work;
             inf.rows = im.rows;
             inf.cols = im.cols;
             inf.tile = it.tile;
@@ -293,10 +299,17 @@ __global__ void __launch_bounds__(kBlock, MINB) fft_batch_ws(BatchArgs a) {
                 const float2 *src = (it.pass == 0 ? im.src : im.dst) + (size_t)row0 * n;
                 mbar_arrive_tx(&sh.full[s], bytes);
                 bulk_g2s(stage, src, bytes, &sh.full[s]);
+            } else if (im.work) {
+                // the previous rows pass left this tile as one contiguous block
+                const int n = im.rows, w = tile_px / n;
+                const unsigned bytes = (unsigned)(n * w * sizeof(float2));
+                mbar_arrive_tx(&sh.full[s], bytes);
+                bulk_g2s(stage, im.work + (size_t)it.tile * n * w, bytes, &sh.full[s]);
             } else {
                 const int n = im.rows, w = tile_px / n;
                 const int br = n < 256 ? n : 256;
-                const void *tmap = static_cast<const unsigned char *>(a.tmaps) + (size_t)it.image * 128;
+                const void *tmap = static_cast<const unsigned char *>(a.tmaps) +
+                                   (size_t)it.image * 128 * kBatchTmapsPerImage;
                 mbar_arrive_tx(&sh.full[s], (unsigned)(n * w * sizeof(float2)));
                 for (int b = 0; b < n / br; b++)
                     tensor2d_g2s(stage + (size_t)b * br * w, tmap, it.tile * w, b * br, &sh.full[s]);
@@ -410,16 +423,20 @@ __global__ void __launch_bounds__(kBlock, MINB) fft_batch_ws(BatchArgs a) {
             const StageInfo inf = sh.info[s];
             if (!inf.valid) break;
             const float2 *stage = stages + (size_t)s * kStageElems;
-            if (inf.along_rows) {
+            const unsigned char *tmaps = static_cast<const unsigned char *>(a.tmaps) +
+                                         (size_t)inf.image * 128 * kBatchTmapsPerImage;
+            if (inf.along_rows && inf.work) {
+                // one box: the tile's rows into the column-tiled layout
+                const int lines = tile_px / inf.cols;
+                tensor3d_s2g(tmaps + 128, 0, 0, inf.tile * lines, stage);
+            } else if (inf.along_rows) {
                 const int n = inf.cols, lines = tile_px / n, row0 = inf.tile * lines;
                 const int nrows = min(lines, inf.rows - row0);
                 bulk_s2g(inf.dst + (size_t)row0 * n, stage, (unsigned)(nrows * n * sizeof(float2)));
             } else {
                 const int n = inf.rows, w = tile_px / n, br = n < 256 ? n : 256;
-                const void *tmap =
-                    static_cast<const unsigned char *>(a.tmaps) + (size_t)inf.image * 128;
                 for (int b = 0; b < n / br; b++)
-                    tensor2d_s2g(tmap, inf.tile * w, b * br, stage + (size_t)b * br * w);
+                    tensor2d_s2g(tmaps, inf.tile * w, b * br, stage + (size_t)b * br * w);
             }
             bulk_commit();
             const unsigned long long tw0 = a.stats ? gtimer() : 0;

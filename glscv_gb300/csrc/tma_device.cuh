@@ -1,5 +1,5 @@
 // tma_device.cuh -- inline PTX for mbarriers and Tensor Memory Accelerator
-// copies (cp.async.bulk, 1-D and 2-D tensor), shared by the persistent batch
+// copies (cp.async.bulk, 1-D, 2-D and 3-D tensor), shared by the persistent batch
 // kernel and the streamed long-line passes.
 #pragma once
 #include <cuda.h>
@@ -82,6 +82,12 @@ __device__ __forceinline__ void tensor2d_s2g(const void *tmap, int x, int y, con
                      tmap),
                  "r"(x), "r"(y), "r"(smem_u32(src))
                  : "memory");
+}
+__device__ __forceinline__ void tensor3d_s2g(const void *tmap, int x, int y, int z, const void *src) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.global.shared::cta.bulk_group [%0, {%1, %2, %3}], [%4];" ::"l"(tmap),
+        "r"(x), "r"(y), "r"(z), "r"(smem_u32(src))
+        : "memory");
 }
 __device__ __forceinline__ void bulk_commit() {
     asm volatile("cp.async.bulk.commit_group;" ::: "memory");

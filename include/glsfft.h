@@ -370,6 +370,18 @@ GLSFFT_API int glsfft_batch_info(glsfft_batch plan, int *persistent_images, int 
                                  int *grid);
 
 /*
+ * The plan's column-tiled workspace: images of the persistent launch with
+ * 4096 <= rows * cols <= 2^20 get one image-sized device buffer each (held
+ * by the plan, freed by glsfft_batch_destroy) when it fits the context's
+ * budget next to the plan's tables.  A rows pass leaves such an image's
+ * result there with its columns tiles contiguous, so the warp-specialised
+ * schedules read every columns tile as one contiguous copy; without it the
+ * columns passes read and write dst in place.  Results are the same either
+ * way.  Reports the images that have one and the bytes held.
+ */
+GLSFFT_API int glsfft_batch_workspace(glsfft_batch plan, int *tiled_images, size_t *bytes);
+
+/*
  * Host-side fault injection for tests: make the last work item wait for one
  * tile more than exists and set the wait deadline to wait_limit_ns, so the
  * next execution reports GLSFFT_ERROR_TIMEOUT instead of finishing cleanly.

@@ -103,6 +103,33 @@ def test_injected_stall_times_out_and_context_survives(ctx, torch_cuda, oracle, 
     assert oracle.rel_l2(y, oracle.fft2d_f64(x)) < 1e-6
 
 
+@pytest.mark.parametrize("inplace", [False, True])
+def test_column_tiled_workspace_same_results(ctx, torch_cuda, inplace):
+    """Images with 4096 <= rows * cols <= 2^20 get a column-tiled workspace
+    (rows passes store there, columns passes read one contiguous block);
+    with a budget that leaves it out, the columns passes work in place.  The
+    results are bit-identical either way, and to the single-image path."""
+    torch = torch_cuda
+    shapes = [(1024, 1024), (512, 256), (16, 4096), (1024, 2048), (64, 32), (128, 128),
+              (256, 16)]
+    flags = (0, INV | SCALE)
+    b, xs, _, _, with_ws = _run_batch(ctx, torch, shapes, flags, variant=3, inplace=inplace)
+    tiled = [(r, c) for r, c in shapes if 4096 <= r * c <= 1 << 20]
+    assert b.workspace() == {"tiled_images": len(tiled), "bytes": sum(8 * r * c for r, c in tiled)}
+    b.close()
+    ctx.set_budget(4 << 20)  # the plan's tables fit, the workspace does not
+    try:
+        b2, _, _, _, without = _run_batch(ctx, torch, shapes, flags, variant=3, inplace=inplace)
+        assert b2.workspace() == {"tiled_images": 0, "bytes": 0}
+        b2.close()
+    finally:
+        ctx.set_budget(0)
+    for i, x in enumerate(xs):
+        assert np.array_equal(with_ws[i].view(np.uint32), without[i].view(np.uint32)), shapes[i]
+        ref = _single(ctx, torch, x, flags)
+        assert np.array_equal(with_ws[i].view(np.uint32), ref.view(np.uint32)), shapes[i]
+
+
 def test_batch_argument_errors(ctx, torch_cuda):
     torch = torch_cuda
     d = torch.zeros((8, 8), dtype=torch.complex64, device="cuda")
