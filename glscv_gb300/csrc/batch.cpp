@@ -204,11 +204,23 @@ int glsfft::make_column_tmap(void *tmap128, const void *img, int rows, int cols)
     return make_tmap_2d(tmap128, img, cols, rows, w, br);
 }
 
-int glsfft::make_tiled_tmap(void *tmap128, const void *work, int rows, int cols) {
+int glsfft::make_tiled_tmap(void *tmap128, const void *work, int rows, int cols, bool swizzled) {
     if (!batch_tiled_ok(rows, cols)) return GLSFFT_ERROR_INVALID_VALUE;
     auto enc = tmap_encoder();
     if (!enc) return GLSFFT_ERROR_CUDA;
     const int w = kBatchTileElems / rows, lines = kBatchTileElems / cols;
+    if (swizzled) {
+        if (!batch_tiled_inplace(rows, cols)) return GLSFFT_ERROR_INVALID_VALUE;
+        cuuint64_t d2[2] = {(cuuint64_t)rows * w, (cuuint64_t)(cols / w)};
+        cuuint64_t s2[1] = {(cuuint64_t)rows * w * sizeof(float2)};
+        cuuint32_t b2[2] = {(cuuint32_t)(lines * w), (cuuint32_t)(cols / w)};
+        cuuint32_t e2[2] = {1, 1};
+        CUresult r2 = enc(reinterpret_cast<CUtensorMap *>(tmap128), CU_TENSOR_MAP_DATA_TYPE_UINT64,
+                          2, const_cast<void *>(work), d2, s2, b2, e2, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                          CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        return r2 == CUDA_SUCCESS ? GLSFFT_SUCCESS : GLSFFT_ERROR_CUDA;
+    }
     cuuint64_t dims[3] = {(cuuint64_t)w, (cuuint64_t)(cols / w), (cuuint64_t)rows};
     cuuint64_t strides[2] = {(cuuint64_t)rows * w * sizeof(float2), (cuuint64_t)w * sizeof(float2)};
     cuuint32_t box[3] = {(cuuint32_t)w, (cuuint32_t)(cols / w), (cuuint32_t)lines};
@@ -314,6 +326,7 @@ int glsfft_batch_create(glsfft_context ctx, int count, const void *const *srcs,
             for (BatchImage &im : plan->images) {
                 if (!batch_tiled_ok(im.rows, im.cols)) continue;
                 im.work = reinterpret_cast<float2 *>(w);
+                im.ws_inplace = batch_tiled_inplace(im.rows, im.cols) ? 1 : 0;
                 w += up(sizeof(float2) * (size_t)im.rows * im.cols);
             }
         }
@@ -324,8 +337,12 @@ int glsfft_batch_create(glsfft_context ctx, int count, const void *const *srcs,
                 unsigned char *tm = host.data() + 128 * kBatchTmapsPerImage * i;
                 st = make_column_tmap(tm, im.dst, im.rows, im.cols);
                 // an encoder that refuses the tiled map leaves the image in place
-                if (!st && im.work && make_tiled_tmap(tm + 128, im.work, im.rows, im.cols))
+                if (!st && im.work &&
+                    (make_tiled_tmap(tm + 128, im.work, im.rows, im.cols, false) ||
+                     (im.ws_inplace && make_tiled_tmap(tm + 256, im.work, im.rows, im.cols, true)))) {
                     im.work = nullptr;
+                    im.ws_inplace = 0;
+                }
             }
             std::memcpy(host.data() + o_im, plan->images.data(), b_im);
             std::memcpy(host.data() + o_ps, plan->passes.data(), b_ps);

@@ -20,15 +20,27 @@ constexpr int kBatchMaxPasses = 4;      // passes per image (2 transforms)
 // Column-tiled layout: with W = kBatchTileElems / rows columns per tile,
 // pixel (r, c) is at work[((c / W) * rows + r) * W + c % W] -- a columns
 // tile is rows * W consecutive pixels, and the W-wide pieces of one row are
-// rows * W apart.  Every pass then reads its tile with one contiguous copy
-// (rows from src or dst, columns from work), and no pass reads a buffer
-// that the same pass writes, so src may still equal dst.
+// rows * W apart.  Two ways to use it:
+//   * `ws_inplace` = 0: every rows pass reads rows (src, then dst) and
+//     stores its tile into work with one 3-D tensor box; every columns pass
+//     reads work and writes dst.  No pass reads a buffer it writes.
+//   * `ws_inplace` = 1 (rows * cols = 2^20, where the L = 4096 / cols rows
+//     of a rows tile make one 128-byte piece in every columns tile): every
+//     intermediate stays in work.  Rows passes store through the 3-D box
+//     as above; a later rows pass loads its tile as one 2-D tensor box of
+//     256 such pieces (128-byte swizzle: piece j's 16-byte chunks permuted
+//     by j % 8), so the rows kernel reads that stage in box order; columns
+//     passes read and write their block in place; only pass 0 reads src and
+//     only the last columns pass writes dst.
+// Either way src may equal dst (pass 0 completes before dst is written).
 struct BatchImage {
     const float2 *src;
     float2 *dst;
     float2 *work;              // column-tiled workspace, or null
     int rows, cols;
     int row_tiles, col_tiles;  // tiles of a rows pass / a columns pass
+    int ws_inplace;            // 1: the intermediates stay in work (see above)
+    int pad;
 };
 
 // One pass of the chain every image runs through.
@@ -102,8 +114,9 @@ int batch_ws_grid(int device, int blocks_per_sm);
 int make_column_tmap(void *tmap128, const void *img, int rows, int cols);
 
 // Tensor maps per image in BatchArgs::tmaps: [0] the column map of dst,
-// [1] the tiled map of work (zeroed when the image has no workspace).
-constexpr int kBatchTmapsPerImage = 2;
+// [1] the 3-D tiled map of work, [2] the swizzled 2-D map of an in-place
+// image's work (zeroed where unused).
+constexpr int kBatchTmapsPerImage = 3;
 
 // Whether an image of this shape uses the column-tiled workspace: whole
 // tiles both ways and one rows tile = one tensor box (W, cols / W, lines),
@@ -113,11 +126,20 @@ __host__ __device__ constexpr bool batch_tiled_ok(int rows, int cols) {
            (long long)rows * cols <= 256LL * kBatchTileElems;
 }
 
-// Build the 3-D tensor map through which a rows pass stores one tile into
-// the column-tiled layout of `work` (rows x cols): dimensions (W, cols / W,
-// rows) with strides (8, rows * W * 8, W * 8) bytes, box (W, cols / W,
-// kBatchTileElems / cols) -- the box lands in shared memory as the tile's
-// rows, one after another.
-int make_tiled_tmap(void *tmap128, const void *work, int rows, int cols);
+// Whether the image keeps every intermediate in its workspace
+// (BatchImage::ws_inplace): a rows tile is 256 pieces of exactly 128 bytes.
+__host__ __device__ constexpr bool batch_tiled_inplace(int rows, int cols) {
+    return batch_tiled_ok(rows, cols) && (long long)rows * cols == 256LL * kBatchTileElems;
+}
+
+// Build a tensor map through which a rows pass moves one tile of the
+// column-tiled layout of `work` (rows x cols).  `swizzled` = false: 3-D,
+// dimensions (W, cols / W, rows) with strides (8, rows * W * 8, W * 8)
+// bytes, box (W, cols / W, 4096 / cols) -- the box lands in shared memory as
+// the tile's rows, one after another.  `swizzled` = true (in-place images
+// only): 2-D, dimensions (rows * W, cols / W) with stride rows * W * 8
+// bytes, box (16, 256), 128-byte swizzle -- a box is the tile's 256 pieces
+// of 128 bytes, piece j's 16-byte chunk c at chunk c ^ (j % 8).
+int make_tiled_tmap(void *tmap128, const void *work, int rows, int cols, bool swizzled);
 
 }  // namespace glsfft

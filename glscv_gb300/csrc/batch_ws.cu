@@ -12,7 +12,11 @@
 //     stored its tile there with one 3-D tensor box), else 2-D boxes through
 //     a per-image tensor map of dst (cp.async.bulk.tensor.2d) -- the column
 //     staging that replaces the reference's separate tiled/untiled copy
-//     passes (glsCV/glsCopy.cpp).
+//     passes (glsCV/glsCopy.cpp);
+//   * an image whose intermediates all stay in the workspace
+//     (BatchImage::ws_inplace) loads a later rows tile as one 128-byte-
+//     swizzled 2-D box of 256 pieces and stores its columns blocks back in
+//     place with cp.async.bulk.
 // Completion of each copy lands on the stage's "full" mbarrier.  The compute
 // warps read their 16 values per thread from the stage, run the Stockham
 // passes (exchanging through the same buffer), write the results back into
@@ -50,8 +54,10 @@ struct StageInfo {
     float2 *work;  // the image's column-tiled workspace, or null
     int rows, cols, tile, image;
     int pass, along_rows, flags, scale;
-    int valid;  // 0: no more work
-    int pad[3];
+    int valid;       // 0: no more work
+    int ws_inplace;  // the image keeps its intermediates in work (BatchImage)
+    int last;        // the image's last pass
+    int pad;
 };
 
 template <int ST>
@@ -72,7 +78,7 @@ __host__ __device__ constexpr bool tw_cached(int n) { return n >= 32 && n <= kTw
 // dynamic shared memory of a block with ST stages
 template <int ST>
 constexpr size_t ws_smem() {
-    return ST * kStageBytes + kTwCacheF4 * sizeof(float4) + sizeof(WsShared<ST>) + 128;
+    return ST * kStageBytes + kTwCacheF4 * sizeof(float4) + sizeof(WsShared<ST>) + 1024;
 }
 
 // ------------------------------------------------------------ compute side
@@ -89,6 +95,20 @@ __device__ __forceinline__ void ws_line(float2 (&x)[16 < N ? 16 : N], int t, Sm 
     }
 }
 
+// Stage position of value t (column t, thread t of the line) of line `l`
+// of a rows tile loaded as one in-place workspace box (N >= 1024
+// points, rows = 2^20 / N): piece j = column / W (W = N / 256) holds the W
+// values of columns tile j of the tile's 4096 / N lines, 16 values = 128
+// bytes, whose 16-byte chunks the 128-byte swizzle permutes by j % 8.
+// Column t + m * (N / 16) lies in piece t / W + 16 m, at this position
+// + 256 m (the swizzle acts on bits 1-3 only).
+template <int N>
+__device__ __forceinline__ unsigned ws_swz_base(unsigned l, unsigned t) {
+    constexpr unsigned W = N / 256;
+    const unsigned j = t / W;
+    return (j * 16 + l * W + t % W) ^ ((j & 7) << 1);
+}
+
 template <int N>
 __device__ __forceinline__ void ws_rows(float2 *stage, const StageInfo &in, const float2 *tw,
                                         const float4 *twc, int tid) {
@@ -97,16 +117,25 @@ __device__ __forceinline__ void ws_rows(float2 *stage, const StageInfo &in, cons
     const int row = in.tile * LINES + l;
     const bool active = row < in.rows;
     const bool cin = in.flags & PF_CONJ_IN, cout = in.flags & PF_CONJ_OUT;
+    // an in-place workspace image: passes after the first stage the tile
+    // in the workspace box's order
     float2 x[E];
-    const float2 *sp = stage + l * N + t;
+    if (N >= 1024 && in.ws_inplace && in.pass > 0) {
+        const unsigned p0 = ws_swz_base<N>(l, t);
 #pragma unroll
-    for (int m = 0; m < E; m++) x[m] = active ? sp[m * T] : make_float2(0.f, 0.f);
+        for (int m = 0; m < E; m++) x[m] = stage[p0 + 256 * m];
+    } else {
+        const float2 *sp = stage + l * N + t;
+#pragma unroll
+        for (int m = 0; m < E; m++) x[m] = active ? sp[m * T] : make_float2(0.f, 0.f);
+    }
     conj_line(x, cin);
     SyncCompute256{}();  // the exchanges below overwrite the staged tile
     ws_line<N>(x, t, RowSm{stage + l * padded_count(N)}, tw, twc);
     finish_line(x, in.scale ? 1.0f / (float)N : 1.0f, cout);
     // results back into the stage as the tile's rows, contiguous, for the
-    // producer's bulk store (after every thread's last exchange read)
+    // producer's bulk store or 3-D box (after every thread's last exchange
+    // read)
     SyncCompute256{}();
     if (active) store_line<N, E, T>(stage + l * N, 1, x, t, in.flags & PF_SHIFT_COLS);
 }
@@ -188,10 +217,12 @@ __device__ __forceinline__ void ws_compute(float2 *stage, const StageInfo &in, c
 template <int MINB, int ST>
 __global__ void __launch_bounds__(kBlock, MINB) fft_batch_ws(BatchArgs a) {
     extern __shared__ __align__(128) unsigned char ws_raw[];
-    // 128-byte aligned stage buffers, the twiddle cache, then the barriers
-    // and stage records (offsetting the shared array itself, not a cast
-    // integer, keeps the compiler's shared-window addressing)
-    unsigned char *base = ws_raw + ((128u - (smem_u32(ws_raw) & 127u)) & 127u);
+    // 1024-byte aligned stage buffers (the 128-byte swizzle of the
+    // in-place workspace boxes follows shared-memory address bits 7-9), the
+    // twiddle cache, then the barriers and stage records (offsetting the
+    // shared array itself, not a cast integer, keeps the compiler's
+    // shared-window addressing)
+    unsigned char *base = ws_raw + ((1024u - (smem_u32(ws_raw) & 1023u)) & 1023u);
     float2 *stages = reinterpret_cast<float2 *>(base);
     float4 *twc = reinterpret_cast<float4 *>(base + ST * kStageBytes);
     WsShared<ST> &sh = *reinterpret_cast<WsShared<ST> *>(base + ST * kStageBytes +
@@ -290,8 +321,16 @@ __global__ void __launch_bounds__(kBlock, MINB) fft_batch_ws(BatchArgs a) {
             inf.flags = ps.flags;
             inf.scale = ps.scale;
             inf.valid = 1;
+            inf.ws_inplace = im.ws_inplace;
+            inf.last = it.pass == a.n_passes - 1;
             float2 *stage = stages + (size_t)s * kStageElems;
-            if (ps.along_rows) {
+            if (ps.along_rows && im.ws_inplace && it.pass > 0) {
+                // the tile's 256 pieces of 128 bytes from the workspace
+                const void *tmap = static_cast<const unsigned char *>(a.tmaps) +
+                                   (size_t)it.image * 128 * kBatchTmapsPerImage + 256;
+                mbar_arrive_tx(&sh.full[s], (unsigned)(tile_px * sizeof(float2)));
+                tensor2d_g2s(stage, tmap, it.tile * 16, 0, &sh.full[s]);
+            } else if (ps.along_rows) {
                 const int n = im.cols, lines = tile_px / n;
                 const int row0 = it.tile * lines;
                 const int nrows = min(lines, im.rows - row0);
@@ -426,13 +465,17 @@ __global__ void __launch_bounds__(kBlock, MINB) fft_batch_ws(BatchArgs a) {
             const unsigned char *tmaps = static_cast<const unsigned char *>(a.tmaps) +
                                          (size_t)inf.image * 128 * kBatchTmapsPerImage;
             if (inf.along_rows && inf.work) {
-                // one box: the tile's rows into the column-tiled layout
+                // one 3-D box: the tile's rows into the column-tiled layout
                 const int lines = tile_px / inf.cols;
                 tensor3d_s2g(tmaps + 128, 0, 0, inf.tile * lines, stage);
             } else if (inf.along_rows) {
                 const int n = inf.cols, lines = tile_px / n, row0 = inf.tile * lines;
                 const int nrows = min(lines, inf.rows - row0);
                 bulk_s2g(inf.dst + (size_t)row0 * n, stage, (unsigned)(nrows * n * sizeof(float2)));
+            } else if (inf.ws_inplace && !inf.last) {
+                // the columns block back in place in the workspace
+                bulk_s2g(inf.work + (size_t)inf.tile * tile_px, stage,
+                         (unsigned)(tile_px * sizeof(float2)));
             } else {
                 const int n = inf.rows, w = tile_px / n, br = n < 256 ? n : 256;
                 for (int b = 0; b < n / br; b++)
