@@ -494,8 +494,9 @@ def precision_form(ctx, torch, s) -> dict:
             del d, o
         row["tc_over_fp32_time"] = round(row["forward_ms"]["tc"] / row["forward_ms"]["fp32"], 3)
         out.append(row)
-    return {"form": "four-step, DFT stages as mma.sync m16n8k16 f16 products with hi/lo split "
-                    "(3 products, FP32 accumulate, separate correction accumulator)",
+    return {"form": "four-step, 32- and 64-point DFT stages as tcgen05.mma kind::f16 products "
+                    "(operands K-major 128-byte-swizzled in shared memory, FP16 hi/lo split: "
+                    "hi*hi and hi*lo + lo*hi in two FP32 tensor-memory accumulators)",
             "kept_as_default": False, "cases": out}
 
 
