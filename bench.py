@@ -71,6 +71,9 @@ def parse():
     p.add_argument("--profile-tc", type=int, default=0, metavar="N",
                    help="run the precision form (split-FP16 tensor-core FFT) forward on --images "
                         "NxN images three times and exit (for ncu)")
+    p.add_argument("--profile-serve", type=int, default=0, metavar="R",
+                   help="set up the serving sweep's references and frames, replay R requests at "
+                        "10k/s in direct frame-read mode once and exit (for ncu)")
     p.add_argument("--profile-fft", type=int, default=0, metavar="N",
                    help="run gls::fft forward on one NxN image three times with the size's "
                         "default pass schedules and exit (for ncu)")
@@ -311,7 +314,7 @@ def shifted_frame_gpu(torch, base, sx: float, sy: float, noise, n: int):
 
 
 def serving_sweep(g, ctx, torch, requests: int = 2000, repeats: int = 3, slots: int = 16,
-                  modes=("direct", "copy")) -> dict:
+                  modes=("direct", "copy"), rates=None, check_alone: bool = True) -> dict:
     """Config 5: Poisson arrivals (seed 5) of CV_32FC1 frame pairs sized 512^2,
     1024^2 or 2048^2 (mix .5/.35/.15) against 32 resident reference spectra
     (16 / 11 / 5 distinct smooth fields); every reference has 4 distinct
@@ -365,13 +368,13 @@ def serving_sweep(g, ctx, torch, requests: int = 2000, repeats: int = 3, slots: 
     # reproduce it); also loads every kernel
     srv.set_frame_read(False)
     alone = {}
-    for i, (n, rid, hb, _) in enumerate(frames):
+    for i, (n, rid, hb, _) in enumerate(frames if check_alone else []):
         for _ in range(2):
             alone[i] = srv.wait(srv.submit(rid, hb.data_ptr()))[0]
     for mode in modes:
         srv.set_frame_read(mode == "direct")
         out["modes"][mode] = {"rates": _serving_rates(srv, frames, by_size, alone, rng, requests,
-                                                      repeats)}
+                                                      repeats, rates)}
     srv.set_frame_read(True)
     out["stats"] = srv.stats()
     srv.close()
@@ -380,11 +383,12 @@ def serving_sweep(g, ctx, torch, requests: int = 2000, repeats: int = 3, slots: 
     return out
 
 
-def _serving_rates(srv, frames, by_size, alone, rng, requests, repeats):
+def _serving_rates(srv, frames, by_size, alone, rng, requests, repeats, rates=None):
     import numpy as np
-    per_rate = {rate: [] for rate in SERVE_RATES}
+    rates = tuple(rates or SERVE_RATES)
+    per_rate = {rate: [] for rate in rates}
     for rep in range(repeats):
-        for rate in SERVE_RATES:
+        for rate in rates:
             offs = np.cumsum(rng.exponential(1.0 / rate, requests))
             cls = rng.choice(len(SERVE_SIZES), size=requests, p=SERVE_MIX)
             pick = [by_size[SERVE_SIZES[c]][int(rng.integers(0, len(by_size[SERVE_SIZES[c]])))]
@@ -396,7 +400,7 @@ def _serving_rates(srv, frames, by_size, alone, rng, requests, repeats):
             err = max(max(abs(r[0] - frames[i][3][0]), abs(r[1] - frames[i][3][1]))
                       for r, i in zip(res, pick))
             dev = max(max(abs(r[0] - alone[i][0]), abs(r[1] - alone[i][1]))
-                      for r, i in zip(res, pick))
+                      for r, i in zip(res, pick)) if alone else None
             span = offs[-1] + lat[-1] / 1e3
             l1024 = lat[[frames[i][0] == 1024 for i in pick]]
             p99 = float(np.percentile(lat, 99))
@@ -417,11 +421,11 @@ def _serving_rates(srv, frames, by_size, alone, rng, requests, repeats):
                                             "gpu_copy"),
                                            [round(float(v), 4) for v in ph[tail].mean(axis=0)])),
                 "max_error_vs_true_shift_px": round(float(err), 4),
-                "max_dev_vs_alone_px": float(dev)})
-    rates = []
-    for rate in SERVE_RATES:
+                "max_dev_vs_alone_px": None if dev is None else float(dev)})
+    out = []
+    for rate in rates:
         runs = per_rate[rate]
-        rates.append({
+        out.append({
             "offered_per_s": rate, "requests": requests,
             "pairs_per_s": [r["pairs_per_s"] for r in runs],
             "p50_ms": [r["p50_ms"] for r in runs],
@@ -433,8 +437,9 @@ def _serving_rates(srv, frames, by_size, alone, rng, requests, repeats):
             "tail_sizes": [r["tail_sizes"] for r in runs],
             "tail_phases_ms": [r["tail_phases_ms"] for r in runs],
             "max_error_vs_true_shift_px": max(r["max_error_vs_true_shift_px"] for r in runs),
-            "max_dev_vs_alone_px": max(r["max_dev_vs_alone_px"] for r in runs)})
-    return rates
+            "max_dev_vs_alone_px": max((r["max_dev_vs_alone_px"] for r in runs
+                                        if r["max_dev_vs_alone_px"] is not None), default=None)})
+    return out
 
 
 def serving_p99_1024(serving: dict | None, mode: str = "direct"):
@@ -862,6 +867,18 @@ def run_own(args) -> None:
 
     if args.serving_only:
         print(json.dumps(serving_sweep(g, ctx, torch, slots=args.serve_slots)), flush=True)
+        ctx.close()
+        return
+
+    if args.profile_serve:
+        # one short replay of the serving mix (no alone pass), for ncu
+        sv = serving_sweep(g, ctx, torch, requests=args.profile_serve, repeats=1,
+                           slots=args.serve_slots, modes=("direct",), rates=(10000,),
+                           check_alone=False)
+        r = sv["modes"]["direct"]["rates"][0]
+        print(json.dumps({"profile_serve": args.profile_serve, "p99_ms": r["p99_ms"],
+                          "max_error_vs_true_shift_px": r["max_error_vs_true_shift_px"]}),
+              flush=True)
         ctx.close()
         return
 

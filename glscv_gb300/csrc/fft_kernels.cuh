@@ -292,10 +292,43 @@ __global__ void __launch_bounds__(LINES *LineFft<N, E>::T)
     }
 
     float2 x[E];
+    bool staged = false;
+    if constexpr ((LD == LD_R1 || LD == LD_R1W) && num_passes(N, MB) > 1 && N >= 4 && N <= 512) {
+        // Real input on lines of up to 512 points (8 or more rows per
+        // block): the block's rows are staged through the exchange buffer
+        // (unused until the first exchange) with 16-byte loads, four times
+        // fewer memory requests in flight per thread than per-element
+        // loads.  Same values, same products: the result is unchanged.
+        // Measured on GB300, phaseCorrelate 512^2: 0.0194 -> 0.0181 ms per
+        // call; at 1024 and 2048 points it was slower, so those keep the
+        // per-element loads.
+        const float *img = reinterpret_cast<const float *>(in);
+        if ((reinterpret_cast<uintptr_t>(img) & 15) == 0) {
+            const int row0 = blockIdx.x * LINES;
+            const int nrows = min(LINES, a.rows - row0);
+            const float4 *s4 = reinterpret_cast<const float4 *>(img + (size_t)row0 * N);
+            for (int i = threadIdx.x; i < nrows * (N / 4); i += LINES * T)
+                smem_raw[i] = __ldg(s4 + i);
+            __syncthreads();
+            const float *sf = reinterpret_cast<const float *>(smem_raw) + l * N;
 #pragma unroll
-    for (int m = 0; m < E; m++) {
-        const int pos = t + m * T;
-        x[m] = active ? load_elem<LD>(in, a.window, (size_t)row * N + pos) : make_float2(0.f, 0.f);
+            for (int m = 0; m < E; m++) {
+                const int pos = t + m * T;
+                float v = active ? sf[pos] : 0.f;
+                if constexpr (LD == LD_R1W)
+                    v = active ? __ldg(a.window + (size_t)row * N + pos) * v : 0.f;
+                x[m] = make_float2(v, 0.f);
+            }
+            __syncthreads();  // the first exchange overwrites the staged rows
+            staged = true;
+        }
+    }
+    if (!staged) {
+#pragma unroll
+        for (int m = 0; m < E; m++) {
+            const int pos = t + m * T;
+            x[m] = active ? load_elem<LD>(in, a.window, (size_t)row * N + pos) : make_float2(0.f, 0.f);
+        }
     }
     conj_line(x, conj_in);
     F::run(x, t, RowSm{smem + l * padded_count(N)}, a.tw);

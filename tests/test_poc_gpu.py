@@ -245,3 +245,30 @@ def test_async_call_captured_in_cuda_graph(ctx, torch_cuda):
     got = res.cpu().numpy()
     (dx, dy), resp = ctx.phase_correlate(da.data_ptr(), db.data_ptr(), w.data_ptr(), n, n, 5)
     assert (got[0], got[1], got[2]) == (dx, dy, resp)
+
+
+@pytest.mark.parametrize("n", [256, 512, 1024])
+def test_unaligned_frames_same_result(ctx, torch_cuda, n):
+    """The windowed row pass stages 16-byte-aligned real frames of lines up
+    to 512 points through shared memory with 16-byte loads and reads other
+    frames element by element: frames 4 bytes past a 16-byte boundary give
+    bit-identical results (and the promoted FFT of one the same spectrum)."""
+    torch = torch_cuda
+    a, b = wl.random_pair(n, n, seed=4300 + n, shift=(9.3, -4.6))
+    w = torch.from_numpy(wl.hann_window(n, n)).cuda()
+    out = []
+    for off in (0, 1):
+        da = torch.zeros(n * n + 4, dtype=torch.float32, device="cuda")
+        db = torch.zeros(n * n + 4, dtype=torch.float32, device="cuda")
+        da[off:off + n * n] = torch.from_numpy(np.ascontiguousarray(a, np.float32)).cuda().view(-1)
+        db[off:off + n * n] = torch.from_numpy(np.ascontiguousarray(b, np.float32)).cuda().view(-1)
+        pa, pb = da[off:].data_ptr(), db[off:].data_ptr()
+        assert (pa % 16 == 0) == (off == 0)
+        out.append(ctx.phase_correlate(pa, pb, w.data_ptr(), n, n, 5))
+        spec = torch.empty((n, n), dtype=torch.complex64, device="cuda")
+        ctx.fft2d(pa, spec.data_ptr(), n, n, 0, torch.cuda.current_stream().cuda_stream,
+                  real_input=True)
+        torch.cuda.synchronize()
+        out.append(spec.cpu().numpy())
+    assert out[0] == out[2]
+    assert np.array_equal(out[1].view(np.uint32), out[3].view(np.uint32))
