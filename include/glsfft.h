@@ -371,9 +371,9 @@ GLSFFT_API int glsfft_batch_info(glsfft_batch plan, int *persistent_images, int 
 
 /*
  * The plan's column-tiled workspace: images of the persistent launch with
- * 4096 <= rows * cols <= 2^20 get one image-sized device buffer each (held
- * by the plan, freed by glsfft_batch_destroy) when it fits the context's
- * budget next to the plan's tables.  A rows pass leaves such an image's
+ * 1024 rows and 16 <= cols <= 1024 get one image-sized device buffer each
+ * (held by the plan, freed by glsfft_batch_destroy) when it fits the
+ * context's budget next to the plan's tables.  A rows pass leaves such an image's
  * result there with its columns tiles contiguous, so the warp-specialised
  * schedules read every columns tile as one contiguous copy; without it the
  * columns passes read and write dst in place.  Results are the same either

@@ -106,17 +106,17 @@ def test_injected_stall_times_out_and_context_survives(ctx, torch_cuda, oracle, 
 @pytest.mark.parametrize("inplace", [False, True])
 @pytest.mark.parametrize("flags", [(0, INV | SCALE), (SHIFT,), (INV, SCALE | SHIFT)])
 def test_column_tiled_workspace_same_results(ctx, torch_cuda, flags, inplace):
-    """Images with 4096 <= rows * cols <= 2^20 get a column-tiled workspace
-    (columns passes read one contiguous block from it; at rows * cols = 2^20
-    every intermediate stays there, rows tiles moving as 128-byte-swizzled
-    boxes); with a budget that leaves it out, the columns passes work in
-    place in dst.  The results are bit-identical either way, and to the
-    single-image path."""
+    """Images of 1024 rows with 16 <= cols <= 1024 get a column-tiled
+    workspace (columns passes read one contiguous block from it; at 1024^2
+    every intermediate stays there, later rows tiles loading as 128-byte-
+    swizzled boxes); with a budget that leaves it out, the columns passes
+    work in place in dst.  The results are bit-identical either way, and to
+    the single-image path."""
     torch = torch_cuda
     shapes = [(1024, 1024), (512, 256), (16, 4096), (1024, 2048), (64, 32), (128, 128),
-              (256, 16), (512, 2048), (256, 4096)]
+              (256, 16), (512, 2048), (1024, 512), (1024, 64), (1024, 16)]
     b, xs, _, _, with_ws = _run_batch(ctx, torch, shapes, flags, variant=3, inplace=inplace)
-    tiled = [(r, c) for r, c in shapes if 4096 <= r * c <= 1 << 20]
+    tiled = [(r, c) for r, c in shapes if r == 1024 and c <= 1024]
     assert b.workspace() == {"tiled_images": len(tiled), "bytes": sum(8 * r * c for r, c in tiled)}
     b.close()
     ctx.set_budget(4 << 20)  # the plan's tables fit, the workspace does not
