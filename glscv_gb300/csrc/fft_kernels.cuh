@@ -208,36 +208,50 @@ __device__ __forceinline__ bool poc_sums_exact(const float *vals, const PocBox &
         cy = (unsigned)(b.minr + lane / w);
     }
     if (!__all_sync(0xffffffffu, ok)) return false;
-    long long q[3];
-    int lo[3];
+    // the three sums' terms, their top and lowest bits, and the warp-wide
+    // extremes: the six reductions run side by side
+    unsigned long long m[3];
+    int top[3], low[3];
 #pragma unroll
     for (int which = 0; which < 3; which++) {
-        const unsigned long long m = mv * (which == 0 ? cx : which == 1 ? cy : 1u);
-        int top = m ? e + (63 - __clzll((long long)m)) : -100000;
-        int low = m ? e : 100000;
-#pragma unroll
-        for (int off = 16; off > 0; off >>= 1) {
-            top = max(top, __shfl_xor_sync(0xffffffffu, top, off));
-            low = min(low, __shfl_xor_sync(0xffffffffu, low, off));
-        }
-        if (low == 100000) {  // every term is zero: the sum is +0
-            q[which] = 0;
-            lo[which] = 0;
-            continue;
-        }
-        if (top - low > 46) return false;
-        const long long t = m ? (long long)(m << (e - low)) : 0;
-        q[which] = neg ? -t : t;
-        lo[which] = low;
+        m[which] = mv * (which == 0 ? cx : which == 1 ? cy : 1u);
+        top[which] = m[which] ? e + (63 - __clzll((long long)m[which])) : -100000;
+        low[which] = m[which] ? e : 100000;
     }
 #pragma unroll
-    for (int which = 0; which < 3; which++) {
-        long long sum = q[which];
+    for (int off = 16; off > 0; off >>= 1) {
 #pragma unroll
-        for (int off = 16; off > 0; off >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, off);
-        // |sum| < 2^53: exact as a double; times the power of two 2^lo, exact
-        const double p2 = __longlong_as_double((long long)(lo[which] + 1023) << 52);
-        if (lane == 0) out3[which] = sum == 0 ? 0.0 : __dmul_rn((double)sum, p2);
+        for (int which = 0; which < 3; which++) {
+            top[which] = max(top[which], __shfl_xor_sync(0xffffffffu, top[which], off));
+            low[which] = min(low[which], __shfl_xor_sync(0xffffffffu, low[which], off));
+        }
+    }
+    bool fits = true;
+#pragma unroll
+    for (int which = 0; which < 3; which++)
+        fits = fits && (low[which] == 100000 || top[which] - low[which] <= 46);
+    if (!fits) return false;
+    // exact integer sums (every term zero: the sum is +0)
+    long long q[3];
+#pragma unroll
+    for (int which = 0; which < 3; which++) {
+        const long long t =
+            (low[which] != 100000 && m[which]) ? (long long)(m[which] << (e - low[which])) : 0;
+        q[which] = neg ? -t : t;
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+#pragma unroll
+        for (int which = 0; which < 3; which++) q[which] += __shfl_xor_sync(0xffffffffu, q[which], off);
+    }
+    if (lane == 0) {
+#pragma unroll
+        for (int which = 0; which < 3; which++) {
+            // |sum| < 2^53: exact as a double; times the power of two 2^lo, exact
+            const int lo = low[which] == 100000 ? 0 : low[which];
+            const double p2 = __longlong_as_double((long long)(lo + 1023) << 52);
+            out3[which] = q[which] == 0 ? 0.0 : __dmul_rn((double)q[which], p2);
+        }
     }
     return true;
 }
