@@ -386,8 +386,12 @@ __global__ void __launch_bounds__(LINES *LineFft<N, E>::T)
                 }
                 __syncthreads();
                 if (s_last) {
+                    // No fence here: every other block's surface stores and
+                    // key update precede its release add (its barrier, then
+                    // thread 0's add), thread 0's acquire add above read the
+                    // final count, and the barrier orders this block's
+                    // reads after that acquire.
                     __shared__ float s_box[kPocBoxCap];
-                    __threadfence();
                     const float *surf = reinterpret_cast<const float *>(out);
                     const PocBox b = poc_box(__ldcg(a.key), a.rows, N, a.box);
                     const int w = b.maxc - b.minc + 1, n = w * (b.maxr - b.minr + 1);
