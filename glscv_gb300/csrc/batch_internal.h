@@ -4,10 +4,11 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "batch_layout.h"
+
 namespace glsfft {
 
 constexpr int kBatchThreads = 256;      // threads of a persistent block
-constexpr int kBatchTileElems = 4096;   // complex values per tile (16 per thread)
 constexpr int kBatchMaxPasses = 4;      // passes per image (2 transforms)
 
 // One image of a batch plan.  Pass 0 reads src; every later pass reads and
@@ -117,29 +118,6 @@ int make_column_tmap(void *tmap128, const void *img, int rows, int cols);
 // [1] the 3-D tiled map of work, [2] the swizzled 2-D map of an in-place
 // image's work (zeroed where unused).
 constexpr int kBatchTmapsPerImage = 3;
-
-// Rows of the shortest columns that get the column-tiled workspace: with
-// 1024-point columns a columns tile is W = 4 columns, 32-byte segments of
-// 1024 rows through the column map; shorter columns have wider tiles
-// (64..512-byte segments) that the map already reads well, and the extra
-// buffer only adds traffic (measured on GB300: 512 uneven images of 128^2 ..
-// 1024^2, forward, 0.749 ms with a workspace for every shape against 0.739
-// without).
-constexpr int kBatchTiledMinRows = 1024;
-
-// Whether an image of this shape uses the column-tiled workspace: whole
-// tiles both ways and one rows tile = one tensor box (W, cols / W, lines),
-// every box dimension <= 256.
-__host__ __device__ constexpr bool batch_tiled_ok(int rows, int cols) {
-    return rows >= kBatchTiledMinRows && cols >= 16 && rows <= 1024 &&
-           (long long)rows * cols >= kBatchTileElems && (long long)rows * cols <= 256LL * kBatchTileElems;
-}
-
-// Whether the image keeps every intermediate in its workspace
-// (BatchImage::ws_inplace): a rows tile is 256 pieces of exactly 128 bytes.
-__host__ __device__ constexpr bool batch_tiled_inplace(int rows, int cols) {
-    return batch_tiled_ok(rows, cols) && (long long)rows * cols == 256LL * kBatchTileElems;
-}
 
 // Build a tensor map through which a rows pass moves one tile of the
 // column-tiled layout of `work` (rows x cols).  `swizzled` = false: 3-D,

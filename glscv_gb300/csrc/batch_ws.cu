@@ -95,20 +95,6 @@ __device__ __forceinline__ void ws_line(float2 (&x)[16 < N ? 16 : N], int t, Sm 
     }
 }
 
-// Stage position of value t (column t, thread t of the line) of line `l`
-// of a rows tile loaded as one in-place workspace box (N >= 1024
-// points, rows = 2^20 / N): piece j = column / W (W = N / 256) holds the W
-// values of columns tile j of the tile's 4096 / N lines, 16 values = 128
-// bytes, whose 16-byte chunks the 128-byte swizzle permutes by j % 8.
-// Column t + m * (N / 16) lies in piece t / W + 16 m, at this position
-// + 256 m (the swizzle acts on bits 1-3 only).
-template <int N>
-__device__ __forceinline__ unsigned ws_swz_base(unsigned l, unsigned t) {
-    constexpr unsigned W = N / 256;
-    const unsigned j = t / W;
-    return (j * 16 + l * W + t % W) ^ ((j & 7) << 1);
-}
-
 template <int N>
 __device__ __forceinline__ void ws_rows(float2 *stage, const StageInfo &in, const float2 *tw,
                                         const float4 *twc, int tid) {
@@ -121,7 +107,7 @@ __device__ __forceinline__ void ws_rows(float2 *stage, const StageInfo &in, cons
     // in the workspace box's order
     float2 x[E];
     if (N >= 1024 && in.ws_inplace && in.pass > 0) {
-        const unsigned p0 = ws_swz_base<N>(l, t);
+        const unsigned p0 = ws_swz_base(N, l, t);
 #pragma unroll
         for (int m = 0; m < E; m++) x[m] = stage[p0 + 256 * m];
     } else {

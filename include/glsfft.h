@@ -353,7 +353,7 @@ GLSFFT_API int glsfft_batch_set_variant(glsfft_batch plan, int variant);
  * claimed, two ahead fetched, the next one's image record and dependency
  * counter read while an item is issued); and the item-list lag (items
  * listed between an image's pass and its next pass; 0 keeps the current
- * order).  Defaults: 2, 0, eight resident grids.
+ * order).  Defaults: 1, 0, four resident grids.
  */
 GLSFFT_API int glsfft_batch_set_schedule(glsfft_batch plan, int claim_chunk, int claim_ahead,
                                          int lag_items);

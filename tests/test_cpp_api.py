@@ -63,3 +63,17 @@ def test_plan_cache_host_unit(tmp_path):
     run = subprocess.run([str(out), str(tmp_path / "cache.jsonl")], capture_output=True,
                          text=True, timeout=60)
     assert run.returncode == 0 and "ALL OK" in run.stdout, run.stdout
+
+
+def test_batch_layout_host_unit(tmp_path):
+    """The batch plans' column-tiled workspace arithmetic (layout, workspace
+    rules, the swizzled stage positions) against emulated tensor boxes,
+    compiled without CUDA."""
+    src = ROOT / "tests" / "cpp" / "test_batch_layout.cpp"
+    out = tmp_path / "test_batch_layout"
+    res = subprocess.run(["g++", "-std=c++17", "-O1", "-Wall",
+                          f"-I{ROOT / 'glscv_gb300' / 'csrc'}", str(src), "-o", str(out)],
+                         capture_output=True, text=True)
+    assert res.returncode == 0, res.stderr
+    run = subprocess.run([str(out)], capture_output=True, text=True, timeout=60)
+    assert run.returncode == 0 and "ALL OK" in run.stdout, run.stdout
