@@ -60,13 +60,14 @@ struct glsfft_batch_s {
 namespace {
 
 // Default schedule: three warp-specialised blocks per SM, items claimed one
-// at a time, an image's next pass listed four resident grids after its
-// previous one -- what the autotuner picks on GB300 for 64 x 1024^2 forward +
-// inverse (lag 4-5) and for 512 uneven images (lag 4), 7 % faster than two
-// items per claim at a lag of eight grids (glsfft_batch_set_schedule / the
-// autotuner can change all).
+// at a time, an image's next pass listed five resident grids after its
+// previous one -- the fastest schedule measured on GB300 for 64 x 1024^2
+// forward + inverse (lag 4 is 0.5 % slower there and 2 % faster on 512
+// uneven images, a difference the autotuner's 1 % keep margin lets it
+// take), 7 % faster than two items per claim at a lag of eight grids
+// (glsfft_batch_set_schedule / the autotuner can change all).
 constexpr int kDefaultClaimChunk = 1;
-constexpr int kDefaultLagGrids = 4;
+constexpr int kDefaultLagGrids = 5;
 
 int row_tiles_of(int rows, int cols) {
     const int lines = kBatchTileElems / cols;

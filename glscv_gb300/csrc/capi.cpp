@@ -391,6 +391,8 @@ int glsfft_context_destroy(glsfft_context ctx) {
     if (!ctx) return GLSFFT_ERROR_INVALID_VALUE;
     DeviceGuard g(ctx->device);
     host_pipe_destroy(ctx->host_pipe);  // its batch plans use the context
+    if (ctx->poc_graph.exec) cudaGraphExecDestroy(ctx->poc_graph.exec);
+    if (ctx->capture_stream) cudaStreamDestroy(ctx->capture_stream);
     if (ctx->ws) cudaFree(ctx->ws);
     if (ctx->d_tw) cudaFree(ctx->d_tw);
     if (ctx->h_result) cudaFreeHost(ctx->h_result);
@@ -561,6 +563,54 @@ int glsfft_phase_correlate_async(glsfft_context ctx, const float *src1, const fl
                       d_result, (cudaStream_t)stream);
 }
 
+// The synchronous call's three launches into the context's mapped result:
+// a replay of the cached graph when the call repeats the last one's
+// buffers, shape and workspace (one graph launch instead of three kernel
+// launches), else the launches captured into a new graph on the context's
+// private stream and that graph launched; if the capture is refused, the
+// launches themselves.
+static int poc_sync_launch(glsfft_context ctx, const float *src1, const float *src2,
+                           const float *window, int rows, int cols, int box, cudaStream_t s) {
+    const size_t n = (size_t)rows * cols;
+    int st = ensure_workspace(ctx, poc_workspace_bytes(rows, cols));
+    if (st) return st;
+    char *ws = static_cast<char *>(ctx->ws);
+    float2 *f1 = reinterpret_cast<float2 *>(ws);
+    float2 *f2 = f1 + n;
+    float *surface = reinterpret_cast<float *>(f2 + n);
+    auto *key = reinterpret_cast<unsigned long long *>(ws + poc_key_offset(rows, cols));
+    ctx->surface = surface;
+    ctx->surface_count = n;
+    auto &pg = ctx->poc_graph;
+    auto same = [&] {
+        return pg.exec && pg.src1 == src1 && pg.src2 == src2 && pg.window == window &&
+               pg.rows == rows && pg.cols == cols && pg.box == box && pg.ws == ctx->ws;
+    };
+    if (!same()) {
+        if (pg.exec) cudaGraphExecDestroy(pg.exec);
+        pg = glsfft_context_s::PocGraph{};
+        if (!ctx->capture_stream &&
+            cudaStreamCreateWithFlags(&ctx->capture_stream, cudaStreamNonBlocking) != cudaSuccess)
+            ctx->capture_stream = nullptr;
+        if (ctx->capture_stream &&
+            cudaStreamBeginCapture(ctx->capture_stream, cudaStreamCaptureModeThreadLocal) ==
+                cudaSuccess) {
+            cudaGraph_t graph = nullptr;
+            st = poc_launch(ctx->d_tw, src1, src2, window, rows, cols, box, f1, f2, surface, key,
+                            ctx->h_result_dev, ctx->capture_stream);
+            const cudaError_t e = cudaStreamEndCapture(ctx->capture_stream, &graph);
+            cudaGraphExec_t exec = nullptr;
+            if (!st && e == cudaSuccess && graph && cudaGraphInstantiate(&exec, graph, 0) == cudaSuccess)
+                pg = {src1, src2, window, rows, cols, box, ctx->ws, exec};
+            if (graph) cudaGraphDestroy(graph);
+        }
+        cudaGetLastError();  // a refused capture leaves no error behind
+    }
+    if (same()) return cuda_status(cudaGraphLaunch(pg.exec, s));
+    return poc_launch(ctx->d_tw, src1, src2, window, rows, cols, box, f1, f2, surface, key,
+                      ctx->h_result_dev, s);
+}
+
 int glsfft_phase_correlate(glsfft_context ctx, const float *src1, const float *src2,
                            const float *window, int rows, int cols, int box, double *dx,
                            double *dy, double *response, void *stream) {
@@ -571,8 +621,7 @@ int glsfft_phase_correlate(glsfft_context ctx, const float *src1, const float *s
     if (!g.ok()) return GLSFFT_ERROR_CUDA;
     // the last block writes the result straight into the context's mapped
     // pinned buffer: no copy back, one synchronisation
-    st = glsfft_phase_correlate_async(ctx, src1, src2, window, rows, cols, box,
-                                      ctx->h_result_dev, stream);
+    st = poc_sync_launch(ctx, src1, src2, window, rows, cols, box, (cudaStream_t)stream);
     if (st) return st;
     cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);
     if (e != cudaSuccess) return cuda_status(e);

@@ -33,6 +33,15 @@ struct glsfft_context_s {
     long long stall_ns = 0;   // glsfft_context_inject_stall (0: off)
     // the reference-arithmetic mode's twiddle tables, per line length
     std::map<int, float2 *> exact_tw;
+    // glsfft_phase_correlate's three launches as a CUDA graph, replayed
+    // while a call repeats the last one's buffers, shape and workspace
+    struct PocGraph {
+        const float *src1 = nullptr, *src2 = nullptr, *window = nullptr;
+        int rows = 0, cols = 0, box = 0;
+        const void *ws = nullptr;
+        cudaGraphExec_t exec = nullptr;
+    } poc_graph;
+    cudaStream_t capture_stream = nullptr;  // private stream the graph is captured on
 };
 
 namespace glsfft {

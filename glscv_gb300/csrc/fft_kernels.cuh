@@ -276,6 +276,70 @@ __device__ __forceinline__ void poc_result(int rows, int cols, const PocBox &b, 
 // block at once (independent L2 reads in flight) before thread 0 sums them
 constexpr int kPocBoxCap = 1024;
 
+// The argmax commit of a row pass that writes the correlation surface
+// (ST_RE_ARGMAX), and, with a.result set, the centroid in the last block to
+// finish.  `best`: this thread's best key; `red`: blockDim.x / 32 shared
+// words; `surface`: the pass's output (rows x N floats).
+template <int N>
+__device__ __forceinline__ void poc_commit_finish(unsigned long long best, unsigned long long *red,
+                                                  const PassArgs &a, const float *surface) {
+    block_argmax_commit(best, red, a.key);
+    if (a.result) {
+        // the last block to finish (every block's surface writes and
+        // key update are released before its count) computes the centroid
+        __shared__ int s_last;
+        if (threadIdx.x == 0) {
+            // one acquire-release add instead of a full fence and a
+            // relaxed add: it releases this block's surface writes
+            // (ordered before it by the barrier in the key commit)
+            // and, in the last block, acquires every other block's
+            unsigned long long prev;
+            asm volatile("atom.acq_rel.gpu.global.add.u64 %0, [%1], 1;"
+                         : "=l"(prev)
+                         : "l"(a.key + 1)
+                         : "memory");
+            s_last = prev == (unsigned long long)gridDim.x * gridDim.y - 1ull;
+        }
+        __syncthreads();
+        if (s_last) {
+            // No fence here: every other block's surface stores and
+            // key update precede its release add (its barrier, then
+            // thread 0's add), thread 0's acquire add above read the
+            // final count, and the barrier orders this block's
+            // reads after that acquire.
+            __shared__ float s_box[kPocBoxCap];
+            const float *surf = surface;
+            const PocBox b = poc_box(__ldcg(a.key), a.rows, N, a.box);
+            const int w = b.maxc - b.minc + 1, n = w * (b.maxr - b.minr + 1);
+            const bool staged = n <= kPocBoxCap;
+            if (staged)
+                for (int i = threadIdx.x; i < n; i += blockDim.x)
+                    s_box[i] = __ldcg(surf + (size_t)(b.minr + i / w) * N + b.minc + i % w);
+            __syncthreads();
+            // the three FP64 sums: exactly on warp 0 when no rounding
+            // can occur, else sequentially on lane 0 of three warps
+            // (separate SM partitions); then thread 0 forms the result
+            // (a result in mapped host memory needs no system fence:
+            // the host reads it after synchronising with the kernel)
+            __shared__ double s_sum[3];
+            __shared__ int s_exact;
+            const int warp = threadIdx.x >> 5, warps = (blockDim.x + 31) >> 5;
+            if (warp == 0) {
+                const bool ex = staged && poc_sums_exact(s_box, b, s_sum);
+                if (threadIdx.x == 0) s_exact = ex;
+            }
+            __syncthreads();
+            if (!s_exact && (threadIdx.x & 31) == 0)
+                for (int which = warp; which < 3; which += warps)
+                    s_sum[which] = poc_sum(surf, N, b, staged ? s_box : nullptr, which);
+            __syncthreads();
+            if ((threadIdx.x & 31) == 0 && (warps >= 3 ? warp < 3 : warp == 0))
+                poc_result(a.rows, N, b, s_sum[0], s_sum[1], s_sum[2], a.result,
+                           warps >= 3 ? warp : -1);
+        }
+    }
+}
+
 // ------------------------------------------------------------- row pass
 // Block: LINES rows x T threads.  blockIdx.y selects the image.  MB bounds
 // the radix (fft_device.cuh).
@@ -366,63 +430,8 @@ __global__ void __launch_bounds__(LINES *LineFft<N, E>::T)
                 best = k > best ? k : best;
             }
         }
-        if constexpr (ST == ST_RE_ARGMAX) {
-            block_argmax_commit(best, red, a.key);
-            if (a.result) {
-                // the last block to finish (every block's surface writes and
-                // key update are released before its count) computes the centroid
-                __shared__ int s_last;
-                if (threadIdx.x == 0) {
-                    // one acquire-release add instead of a full fence and a
-                    // relaxed add: it releases this block's surface writes
-                    // (ordered before it by the barrier in the key commit)
-                    // and, in the last block, acquires every other block's
-                    unsigned long long prev;
-                    asm volatile("atom.acq_rel.gpu.global.add.u64 %0, [%1], 1;"
-                                 : "=l"(prev)
-                                 : "l"(a.key + 1)
-                                 : "memory");
-                    s_last = prev == (unsigned long long)gridDim.x * gridDim.y - 1ull;
-                }
-                __syncthreads();
-                if (s_last) {
-                    // No fence here: every other block's surface stores and
-                    // key update precede its release add (its barrier, then
-                    // thread 0's add), thread 0's acquire add above read the
-                    // final count, and the barrier orders this block's
-                    // reads after that acquire.
-                    __shared__ float s_box[kPocBoxCap];
-                    const float *surf = reinterpret_cast<const float *>(out);
-                    const PocBox b = poc_box(__ldcg(a.key), a.rows, N, a.box);
-                    const int w = b.maxc - b.minc + 1, n = w * (b.maxr - b.minr + 1);
-                    const bool staged = n <= kPocBoxCap;
-                    if (staged)
-                        for (int i = threadIdx.x; i < n; i += blockDim.x)
-                            s_box[i] = __ldcg(surf + (size_t)(b.minr + i / w) * N + b.minc + i % w);
-                    __syncthreads();
-                    // the three FP64 sums: exactly on warp 0 when no rounding
-                    // can occur, else sequentially on lane 0 of three warps
-                    // (separate SM partitions); then thread 0 forms the result
-                    // (a result in mapped host memory needs no system fence:
-                    // the host reads it after synchronising with the kernel)
-                    __shared__ double s_sum[3];
-                    __shared__ int s_exact;
-                    const int warp = threadIdx.x >> 5, warps = (blockDim.x + 31) >> 5;
-                    if (warp == 0) {
-                        const bool ex = staged && poc_sums_exact(s_box, b, s_sum);
-                        if (threadIdx.x == 0) s_exact = ex;
-                    }
-                    __syncthreads();
-                    if (!s_exact && (threadIdx.x & 31) == 0)
-                        for (int which = warp; which < 3; which += warps)
-                            s_sum[which] = poc_sum(surf, N, b, staged ? s_box : nullptr, which);
-                    __syncthreads();
-                    if ((threadIdx.x & 31) == 0 && (warps >= 3 ? warp < 3 : warp == 0))
-                        poc_result(a.rows, N, b, s_sum[0], s_sum[1], s_sum[2], a.result,
-                                   warps >= 3 ? warp : -1);
-                }
-            }
-        }
+        if constexpr (ST == ST_RE_ARGMAX)
+            poc_commit_finish<N>(best, red, a, reinterpret_cast<const float *>(out));
     }
 }
 

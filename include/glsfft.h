@@ -353,7 +353,7 @@ GLSFFT_API int glsfft_batch_set_variant(glsfft_batch plan, int variant);
  * claimed, two ahead fetched, the next one's image record and dependency
  * counter read while an item is issued); and the item-list lag (items
  * listed between an image's pass and its next pass; 0 keeps the current
- * order).  Defaults: 1, 0, four resident grids.
+ * order).  Defaults: 1, 0, five resident grids.
  */
 GLSFFT_API int glsfft_batch_set_schedule(glsfft_batch plan, int claim_chunk, int claim_ahead,
                                          int lag_items);
@@ -446,7 +446,10 @@ GLSFFT_API int glsfft_batch_destroy(glsfft_batch plan);
  * Writes the shift of src2 relative to src1 and the response
  * (sum over the box / (rows*cols)); dx/dy/response are host pointers
  * (response may be NULL).  Synchronises `stream`.  Uses the context workspace
- * (20 * rows * cols bytes).
+ * (20 * rows * cols bytes).  The three launches are kept as a CUDA graph and
+ * replayed while a call repeats the last call's src1, src2, window, shape,
+ * box and workspace (the buffers' contents may change); any other call
+ * captures them anew.  Not to be called from inside a stream capture.
  */
 GLSFFT_API int glsfft_phase_correlate(glsfft_context ctx, const float *src1, const float *src2,
                                       const float *window, int rows, int cols, int box,

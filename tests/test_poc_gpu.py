@@ -272,3 +272,41 @@ def test_unaligned_frames_same_result(ctx, torch_cuda, n):
         out.append(spec.cpu().numpy())
     assert out[0] == out[2]
     assert np.array_equal(out[1].view(np.uint32), out[3].view(np.uint32))
+
+
+def test_sync_call_graph_cache_follows_buffers(ctx, torch_cuda):
+    """The synchronous call replays a cached graph of its three launches
+    while a call repeats the last one's buffers, shape and workspace.  A
+    sequence that changes pairs, sizes and windows, and rewrites a buffer in
+    place, must give the asynchronous path's result at every step."""
+    torch = torch_cuda
+    s = torch.cuda.current_stream().cuda_stream
+    bufs = {}
+    for name, n, seed in (("A", 256, 61), ("B", 256, 62), ("C", 512, 63)):
+        a, b = wl.random_pair(n, n, seed=seed, shift=(5.4, -3.2))
+        bufs[name] = (n, torch.from_numpy(np.ascontiguousarray(a, np.float32)).cuda(),
+                      torch.from_numpy(np.ascontiguousarray(b, np.float32)).cuda(),
+                      torch.from_numpy(wl.hann_window(n, n)).cuda())
+    res = torch.zeros(8, dtype=torch.float64, device="cuda")
+
+    def both(name, window=True):
+        n, da, db, dw = bufs[name]
+        w = dw.data_ptr() if window else None
+        (dx, dy), resp = ctx.phase_correlate(da.data_ptr(), db.data_ptr(), w, n, n, 5, s)
+        ctx.phase_correlate_async(da.data_ptr(), db.data_ptr(), w, n, n, 5, res.data_ptr(), s)
+        torch.cuda.synchronize()
+        got = res.cpu().numpy()
+        assert (dx, dy, resp) == (got[0], got[1], got[2]), name
+
+    for step in ("A", "A", "B", "A", "C", "C", "B"):
+        both(step)
+    both("A", window=False)
+    both("A")
+    # same pointers, new content: the replayed graph reads the buffers anew
+    n, da, db, dw = bufs["A"]
+    a2, b2 = wl.random_pair(n, n, seed=64, shift=(-7.1, 2.6))
+    da.copy_(torch.from_numpy(np.ascontiguousarray(a2, np.float32)).cuda())
+    db.copy_(torch.from_numpy(np.ascontiguousarray(b2, np.float32)).cuda())
+    both("A")
+    (dx, dy), _ = ctx.phase_correlate(da.data_ptr(), db.data_ptr(), dw.data_ptr(), n, n, 5, s)
+    assert abs(abs(dx) - 7.1) < 0.5 and abs(abs(dy) - 2.6) < 0.5
