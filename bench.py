@@ -732,7 +732,9 @@ def plain_single(ctx, torch, s) -> dict:
     """The plain drop-in path one image at a time (gls::fft per call): the
     256^2 forward + inverse(SCALE) case and single 1024^2 / 4096^2 images
     (uniform[-1,1) complex, seeds 0, 1, 2), CUDA events (median of 20 calls
-    after 3), with the error against an FP64 DFT."""
+    after 3, each bracketed by its own events, and 20 calls back to back),
+    with the error against an FP64 DFT.  Uses the context's pass schedules
+    (tuned for 1024^2 by the main run)."""
     import numpy as np
     from glscv_gb300 import workloads as wl
     out = {}
@@ -761,11 +763,23 @@ def plain_single(ctx, torch, s) -> dict:
             ts.append(e0.elapsed_time(e1))
         ts.sort()
         ms = ts[len(ts) // 2]
+        # 20 calls back to back between two events: the device time per call
+        # without the host's launch latency in front of the first kernel
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(20):
+            step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms_b2b = e0.elapsed_time(e1) / 20
         f64 = np.fft.fft2(x.astype(np.complex128))
         fh, yh = f.cpu().numpy(), y.cpu().numpy()
         flops = 2 * 5.0 * n * n * np.log2(n * n)
         out[f"{n}x{n}"] = {
             "fwd_inv_ms": round(ms, 4), "gflops": round(flops / (ms * 1e-3) / 1e9, 1),
+            "fwd_inv_ms_back_to_back": round(ms_b2b, 4),
+            "schedule": list(ctx.get_fft_schedule(n, n)),
             "alg_gbs": round(2 * 32.0 * n * n / (ms * 1e-3) / 1e9, 1),
             "rel_l2_forward_vs_fp64": float(np.linalg.norm(fh - f64) / np.linalg.norm(f64)),
             "rel_l2_round_trip": float(np.linalg.norm(yh - x) / np.linalg.norm(x))}
@@ -827,6 +841,12 @@ def run_own(args) -> None:
         tt = time.perf_counter()
         tune = plan.autotune(None, reps=5, stream=s)
         tune["seconds"] = round(time.perf_counter() - tt, 3)
+    # the plain path's pass schedules for this size, tuned as a user of the
+    # drop-in path would (glsfft_autotune_fft2d), so that the batch plan is
+    # compared with the best plain path
+    plain_tune = None
+    if not (args.no_autotune or args.profile_only or args.schedule):
+        plain_tune = ctx.autotune_fft2d(ROWS, COLS, stream=s)
     launches_per_step = 1
     ev = {}
     base_in, base_out = d_in.data_ptr(), d_out.data_ptr()
@@ -1088,7 +1108,8 @@ def run_own(args) -> None:
             "tc_over_fp32": {c["shape"]: c["tc_over_fp32_time"] for c in precision["cases"]},
             "plain_per_image": {"value": round(plain_value, 3), "unit": UNIT,
                                 "ms_per_step": round(plain_ms, 4),
-                                "speedup_of_value": round(value / plain_value, 3)},
+                                "speedup_of_value": round(value / plain_value, 3),
+                                "pass_schedules": plain_tune},
             "two_launch_batched": {"value": round(two_value, 3), "unit": UNIT,
                                    "ms_per_step": round(two_ms, 4)},
             "rel_l2_vs_fp64": {"forward": rel_fwd, "round_trip": rel_rt},
