@@ -19,6 +19,7 @@
 #include <vector>
 
 #include "batch_internal.h"
+#include "batch_order.h"
 #include "capi_internal.h"
 #include "fft_config.h"
 #include "glsfft_internal.h"
@@ -78,41 +79,9 @@ int col_tiles_of(int rows, int cols) {
     return (cols + w - 1) / w;
 }
 
-// Item order: pass 0 of the images in order; pass p+1 of an image enters the
-// list once `lag` items have been listed after its pass p (the work resident
-// blocks are busy with in the meantime), so its inputs are fresh in L2 and
-// rarely still being written.
 std::vector<BatchItem> order_items(const std::vector<BatchImage> &ims,
                                    const std::vector<BatchPass> &passes, int lag) {
-    struct Pending {
-        size_t ready_at;
-        int image, pass, need;
-    };
-    std::vector<BatchItem> out;
-    std::deque<Pending> pend;  // ready_at is non-decreasing in push order
-    auto tiles = [&](int i, int p) {
-        return passes[p].along_rows ? ims[i].row_tiles : ims[i].col_tiles;
-    };
-    auto emit = [&](int i, int p, int need) {
-        const int n = tiles(i, p);
-        for (int t = 0; t < n; t++) out.push_back(BatchItem{i, p, t, need});
-        if (p + 1 < (int)passes.size())
-            pend.push_back(Pending{out.size() + (size_t)lag, i, p + 1, n});
-    };
-    for (int i = 0; i < (int)ims.size(); i++) {
-        while (!pend.empty() && pend.front().ready_at <= out.size()) {
-            Pending q = pend.front();
-            pend.pop_front();
-            emit(q.image, q.pass, q.need);
-        }
-        emit(i, 0, 0);
-    }
-    while (!pend.empty()) {
-        Pending q = pend.front();
-        pend.pop_front();
-        emit(q.image, q.pass, q.need);
-    }
-    return out;
+    return order_work<BatchItem>(ims, passes, lag);
 }
 
 int grid_for(int device, int variant) {

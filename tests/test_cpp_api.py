@@ -77,3 +77,17 @@ def test_batch_layout_host_unit(tmp_path):
     assert res.returncode == 0, res.stderr
     run = subprocess.run([str(out)], capture_output=True, text=True, timeout=60)
     assert run.returncode == 0 and "ALL OK" in run.stdout, run.stdout
+
+
+def test_batch_order_host_unit(tmp_path):
+    """The batch plans' work-list order: every tile listed once, every item
+    after all tiles of its image's previous pass (no wait on an unclaimed
+    item), over random batches and lags, compiled without CUDA."""
+    src = ROOT / "tests" / "cpp" / "test_batch_order.cpp"
+    out = tmp_path / "test_batch_order"
+    res = subprocess.run(["g++", "-std=c++17", "-O1", "-Wall",
+                          f"-I{ROOT / 'glscv_gb300' / 'csrc'}", str(src), "-o", str(out)],
+                         capture_output=True, text=True)
+    assert res.returncode == 0, res.stderr
+    run = subprocess.run([str(out)], capture_output=True, text=True, timeout=120)
+    assert run.returncode == 0 and "ALL OK" in run.stdout, run.stdout
