@@ -169,6 +169,19 @@ struct MinMaxRun {
     }
 };
 
+// The key reset in front of minmax_kernel: launched in stream order (so no
+// earlier reader of the keys can still be running), it lets the min / max
+// pass, launched as its programmatic dependent, start streaming at once.
+__global__ void minmax_reset_kernel(unsigned long long *keys) {
+    keys[0] = 0ull;
+    keys[1] = 0ull;
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+// The input was complete before the reset kernel started (stream order);
+// only the keys come from it, so the pass waits for its predecessor grid
+// (griddepcontrol.wait, a no-op without programmatic launch) just before it
+// commits them.
 __global__ void __launch_bounds__(kThreads) minmax_kernel(const float *__restrict__ x, size_t n,
                                                           unsigned long long *keys) {
     __shared__ unsigned long long red[2 * (kThreads / 32)];
@@ -203,6 +216,7 @@ __global__ void __launch_bounds__(kThreads) minmax_kernel(const float *__restric
         done = nv * 4;
     }
     for (size_t i = done + tid; i < n; i += stride) run.add(x[i], (unsigned)i);
+    asm volatile("griddepcontrol.wait;" ::: "memory");  // the keys are reset
     run.commit(red, keys);
 }
 
@@ -343,11 +357,11 @@ int glsfft_min_max_loc_async(glsfft_context ctx, const float *src, int rows, int
     DeviceGuard g(ctx->device);
     if (!g.ok()) return GLSFFT_ERROR_CUDA;
     const size_t n = (size_t)rows * cols;
-    cudaError_t e = cudaMemsetAsync(d_keys, 0, 2 * sizeof(unsigned long long), (cudaStream_t)stream);
+    minmax_reset_kernel<<<1, 1, 0, (cudaStream_t)stream>>>(d_keys);
+    cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_status(e);
-    minmax_kernel<<<grid_for(minmax_kernel, n / 4), kThreads, 0, (cudaStream_t)stream>>>(src, n,
-                                                                                         d_keys);
-    return cuda_status(cudaGetLastError());
+    return cuda_status(launch_maybe_pdl(true, minmax_kernel, grid_for(minmax_kernel, n / 4),
+                                        kThreads, 0, (cudaStream_t)stream, src, n, d_keys));
 }
 
 int glsfft_min_max_loc(glsfft_context ctx, const float *src, int rows, int cols,
