@@ -3,6 +3,8 @@
 // gls::phaseCorrelate.
 #include "glsfft.h"
 
+#include <atomic>
+#include <chrono>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -253,7 +255,7 @@ int glsfft::fft2d_launch(glsfft_context ctx, const void *src, void *dst, int row
 int glsfft::poc_launch(const float2 *tw, const float *src1, const float *src2,
                        const float *window, int rows, int cols, int box, float2 *f1, float2 *f2,
                        float *surface, unsigned long long *key, double *d_result,
-                       cudaStream_t s) {
+                       cudaStream_t s, unsigned long long *done_flag) {
     // three launches: rows of both images; fused POC columns (which also
     // zero the argmax key and block counter); inverse rows with the argmax
     // and, in the last block, the centroid.  All three use programmatic
@@ -297,6 +299,7 @@ int glsfft::poc_launch(const float2 *tw, const float *src1, const float *src2,
     c.tw = tw;
     c.result = d_result;
     c.box = box;
+    c.done_flag = done_flag;
     c.pdl = 1;
     e = launch_rows(cols, LD_C2, ST_RE_ARGMAX, c, 1, s);
     return cuda_status(e);
@@ -574,6 +577,9 @@ static int poc_sync_launch(glsfft_context ctx, const float *src1, const float *s
     const size_t n = (size_t)rows * cols;
     int st = ensure_workspace(ctx, poc_workspace_bytes(rows, cols));
     if (st) return st;
+    // the completion flag in the mapped result buffer (double 7, past the
+    // five result values)
+    unsigned long long *flag = reinterpret_cast<unsigned long long *>(ctx->h_result_dev + 7);
     char *ws = static_cast<char *>(ctx->ws);
     float2 *f1 = reinterpret_cast<float2 *>(ws);
     float2 *f2 = f1 + n;
@@ -597,7 +603,7 @@ static int poc_sync_launch(glsfft_context ctx, const float *src1, const float *s
                 cudaSuccess) {
             cudaGraph_t graph = nullptr;
             st = poc_launch(ctx->d_tw, src1, src2, window, rows, cols, box, f1, f2, surface, key,
-                            ctx->h_result_dev, ctx->capture_stream);
+                            ctx->h_result_dev, ctx->capture_stream, flag);
             const cudaError_t e = cudaStreamEndCapture(ctx->capture_stream, &graph);
             cudaGraphExec_t exec = nullptr;
             if (!st && e == cudaSuccess && graph && cudaGraphInstantiate(&exec, graph, 0) == cudaSuccess)
@@ -608,7 +614,7 @@ static int poc_sync_launch(glsfft_context ctx, const float *src1, const float *s
     }
     if (same()) return cuda_status(cudaGraphLaunch(pg.exec, s));
     return poc_launch(ctx->d_tw, src1, src2, window, rows, cols, box, f1, f2, surface, key,
-                      ctx->h_result_dev, s);
+                      ctx->h_result_dev, s, flag);
 }
 
 int glsfft_phase_correlate(glsfft_context ctx, const float *src1, const float *src2,
@@ -619,12 +625,35 @@ int glsfft_phase_correlate(glsfft_context ctx, const float *src1, const float *s
     if (st) return st;
     DeviceGuard g(ctx->device);
     if (!g.ok()) return GLSFFT_ERROR_CUDA;
-    // the last block writes the result straight into the context's mapped
-    // pinned buffer: no copy back, one synchronisation
+    // The last block writes the result straight into the context's mapped
+    // pinned buffer and then sets the completion flag there: the host spins
+    // on the flag (no copy back; it returns as soon as the result is out,
+    // without waiting for the kernel's exit to reach the stream), asking the
+    // stream every 20 us whether it ended or failed first -- then the
+    // stream's own synchronisation reports it.
+    volatile unsigned long long *flag = reinterpret_cast<unsigned long long *>(ctx->h_result + 7);
+    *flag = 0ull;
     st = poc_sync_launch(ctx, src1, src2, window, rows, cols, box, (cudaStream_t)stream);
     if (st) return st;
-    cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);
-    if (e != cudaSuccess) return cuda_status(e);
+    bool seen = false;
+    auto next_query = std::chrono::steady_clock::now() + std::chrono::microseconds(20);
+    for (;;) {
+        if (*flag) {
+            seen = true;
+            break;
+        }
+        const auto now = std::chrono::steady_clock::now();
+        if (now >= next_query) {
+            if (cudaStreamQuery((cudaStream_t)stream) != cudaErrorNotReady) break;
+            next_query = now + std::chrono::microseconds(20);
+        }
+    }
+    if (seen) {
+        std::atomic_thread_fence(std::memory_order_acquire);  // the results after the flag
+    } else {
+        cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);
+        if (e != cudaSuccess) return cuda_status(e);
+    }
     *dx = ctx->h_result[0];
     *dy = ctx->h_result[1];
     if (response) *response = ctx->h_result[2];

@@ -74,7 +74,8 @@ int fft2d_exact_launch(glsfft_context ctx, const void *src, void *dst, void *tmp
 constexpr int kMaxBatch = 65535;  // grid y extent
 int poc_launch(const float2 *tw, const float *src1, const float *src2, const float *window,
                int rows, int cols, int box, float2 *f1, float2 *f2, float *surface,
-               unsigned long long *key, double *d_result, cudaStream_t s);
+               unsigned long long *key, double *d_result, cudaStream_t s,
+               unsigned long long *done_flag = nullptr);
 
 void host_pipe_destroy(HostPipe *p);  // waits for its streams, frees everything
 

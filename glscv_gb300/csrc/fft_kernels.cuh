@@ -336,6 +336,14 @@ __device__ __forceinline__ void poc_commit_finish(unsigned long long best, unsig
             if ((threadIdx.x & 31) == 0 && (warps >= 3 ? warp < 3 : warp == 0))
                 poc_result(a.rows, N, b, s_sum[0], s_sum[1], s_sum[2], a.result,
                            warps >= 3 ? warp : -1);
+            if (a.done_flag) {
+                // the three warps' result stores, then (system scope) the flag
+                __syncthreads();
+                if (threadIdx.x == 0) {
+                    __threadfence_system();
+                    *reinterpret_cast<volatile unsigned long long *>(a.done_flag) = 1ull;
+                }
+            }
         }
     }
 }

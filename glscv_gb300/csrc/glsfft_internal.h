@@ -56,6 +56,9 @@ struct PassArgs {
     // the block counter (zeroed, with key[0], by the POC column pass)
     double *result;
     int box;
+    // with `result`: set to 1 (after a system-scope fence) once result[0..4]
+    // are written, for a host that waits on it instead of the stream; or null
+    unsigned long long *done_flag;
     // device status word for bounded waits (the streamed passes record
     // GLSFFT_ERROR_TIMEOUT there), or null
     int *err;

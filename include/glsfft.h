@@ -445,7 +445,11 @@ GLSFFT_API int glsfft_batch_destroy(glsfft_batch plan);
  * NULL.  box: centroid box edge (the reference uses 5, glsPhaseCorrelate.cpp:219).
  * Writes the shift of src2 relative to src1 and the response
  * (sum over the box / (rows*cols)); dx/dy/response are host pointers
- * (response may be NULL).  Synchronises `stream`.  Uses the context workspace
+ * (response may be NULL).  Returns once the result is written: every
+ * operation issued to `stream` before the call has completed and the call's
+ * kernels have finished with the inputs and the workspace (the last one's
+ * exit may trail by microseconds); a failed kernel is reported through the
+ * stream's synchronisation.  Uses the context workspace
  * (20 * rows * cols bytes).  The three launches are kept as a CUDA graph and
  * replayed while a call repeats the last call's src1, src2, window, shape,
  * box and workspace (the buffers' contents may change); any other call
