@@ -132,6 +132,26 @@ def test_column_tiled_workspace_same_results(ctx, torch_cuda, flags, inplace):
         assert np.array_equal(with_ws[i].view(np.uint32), ref.view(np.uint32)), shapes[i]
 
 
+def test_variant_switch_on_a_workspace_plan(ctx, torch_cuda):
+    """One plan with column-tiled workspaces executed under every variant in
+    turn (the plain kernel ignores the workspace, the warp-specialised ones
+    use it): the same bits each time."""
+    torch = torch_cuda
+    shapes = [(1024, 1024), (1024, 256), (256, 256)]
+    b, xs, d_in, d_out, first = _run_batch(ctx, torch, shapes, (0, INV | SCALE), variant=3)
+    assert b.workspace()["tiled_images"] == 2
+    s = torch.cuda.current_stream().cuda_stream
+    for v in (0, 1, 3, 2, 0, 3):
+        for d in d_out:
+            d.zero_()
+        b.set_variant(v)
+        b.execute(s)
+        assert b.status(s) == 0
+        for i, d in enumerate(d_out):
+            assert np.array_equal(d.cpu().numpy().view(np.uint32), first[i].view(np.uint32)), (v, i)
+    b.close()
+
+
 def test_batch_argument_errors(ctx, torch_cuda):
     torch = torch_cuda
     d = torch.zeros((8, 8), dtype=torch.complex64, device="cuda")

@@ -289,11 +289,11 @@ def test_sync_call_graph_cache_follows_buffers(ctx, torch_cuda):
                       torch.from_numpy(wl.hann_window(n, n)).cuda())
     res = torch.zeros(8, dtype=torch.float64, device="cuda")
 
-    def both(name, window=True):
+    def both(name, window=True, box=5):
         n, da, db, dw = bufs[name]
         w = dw.data_ptr() if window else None
-        (dx, dy), resp = ctx.phase_correlate(da.data_ptr(), db.data_ptr(), w, n, n, 5, s)
-        ctx.phase_correlate_async(da.data_ptr(), db.data_ptr(), w, n, n, 5, res.data_ptr(), s)
+        (dx, dy), resp = ctx.phase_correlate(da.data_ptr(), db.data_ptr(), w, n, n, box, s)
+        ctx.phase_correlate_async(da.data_ptr(), db.data_ptr(), w, n, n, box, res.data_ptr(), s)
         torch.cuda.synchronize()
         got = res.cpu().numpy()
         assert (dx, dy, resp) == (got[0], got[1], got[2]), name
@@ -301,6 +301,9 @@ def test_sync_call_graph_cache_follows_buffers(ctx, torch_cuda):
     for step in ("A", "A", "B", "A", "C", "C", "B"):
         both(step)
     both("A", window=False)
+    both("A")
+    both("A", box=3)
+    both("A", box=7)
     both("A")
     # same pointers, new content: the replayed graph reads the buffers anew
     n, da, db, dw = bufs["A"]
