@@ -23,6 +23,7 @@ def _host(torch, arr):
 @pytest.mark.parametrize("shape,count,chunk,flags", [
     ((256, 512), 10, 4, (0,)),          # two full chunks and a tail of two
     ((1024, 1024), 7, 0, (SHIFT,)),     # automatic chunk
+    ((256, 256), 40, 0, (0, INV | SCALE)),  # automatic chunk (10 images), two transforms
     ((64, 2048), 9, 3, (INV | SCALE,)),
     ((2048, 2048), 3, 1, (0,)),         # images outside the persistent kernel
 ])
@@ -36,7 +37,9 @@ def test_host_pipeline_bit_identical_to_device_path(torch_cuda, shape, count, ch
                      stream_handle(torch))
         torch.cuda.synchronize()
         for i in range(count):
-            ref = gpu_fft(c, torch, xs[i], flags[0])
+            ref = xs[i]
+            for f in flags:  # the chain of transforms, one device call each
+                ref = gpu_fft(c, torch, ref, f)
             assert np.array_equal(h_out[i].numpy().view(np.uint32), ref.view(np.uint32)), i
     assert np.array_equal(h_in.numpy(), xs)  # the input is left alone
 
