@@ -840,7 +840,11 @@ def run_own(args) -> None:
         plan.set_variant(v)
         plan.set_schedule(c, ah, lg * plan.info()["grid"])
         tune = {"fixed": plan.schedule()}
-    elif not (args.no_autotune or args.profile_only):
+    # the single-purpose modes (ncu recipes, the serving sweep alone) tune
+    # nothing: their launch lists must hold only the calls they profile
+    profiling = bool(args.profile_only or args.profile_pc or args.profile_tc or args.profile_fft
+                     or args.profile_spectrum or args.profile_serve or args.serving_only)
+    if not (args.schedule or args.no_autotune or profiling):
         tt = time.perf_counter()
         tune = plan.autotune(None, reps=5, stream=s)
         tune["seconds"] = round(time.perf_counter() - tt, 3)
@@ -848,7 +852,7 @@ def run_own(args) -> None:
     # drop-in path would (glsfft_autotune_fft2d), so that the batch plan is
     # compared with the best plain path
     plain_tune = None
-    if not (args.no_autotune or args.profile_only or args.schedule):
+    if not (args.no_autotune or profiling or args.schedule):
         plain_tune = ctx.autotune_fft2d(ROWS, COLS, stream=s)
     launches_per_step = 1
     ev = {}
